@@ -1,0 +1,352 @@
+#!/usr/bin/env python3
+"""Benchmark of the D3Q19 BGK lid-driven-cavity step on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload: the 512^3 cavity of the headline metric (MLUPS and %HBM peak at
+512^3 for 16-bit storage vs FP32 vs FP64).  A "step" is one lattice-Boltzmann
+iteration over the whole lattice.  The headline value is the FP16-deviation
+storage kernel (nu = 0.005, lid u = 0.08, N(0, 1e-4) seeded noise); BF16,
+FP32 and FP64 are measured in the same run and reported under "modes".
+
+Timing: W untimed iterations, then K iterations bracketed by CUDA events
+recorded on the library's own stream, with a device synchronisation (and, for
+N > 1, a barrier) on both sides; the max over ranks is reported.  Each
+lattice is 10-41 GB, far larger than the 129 MB L2, so no L2 flush is needed
+between iterations.  SM clocks are sampled with nvidia-smi during the timed
+region.
+
+--impl reference times the reference algorithm on the host CPU instead (the
+oracle's C restatement of kernels.cl with OpenMP on all host threads; the
+reference's own OpenCL CPU runtime is not installable here), each step a
+bounded z-slab sample of the same 512^3 FP32 lattice.
+
+N > 1 (torchrun): every rank runs its own replica on its own GPU (the
+reference is single-device; there is no data exchange); value is the sum of
+all replicas' lattice updates over the max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "MLUPS & %HBM peak at 512³: FP16-store vs FP32 vs FP64; adjoint/forward time"
+BYTES_PER_SITE = {"fp16": 76, "bf16": 76, "fp32": 152, "fp64": 304}
+WORKLOAD = dict(dim=512, viscosity=0.005, velocity=0.08, seed=1234, noise_sigma=1e-4)
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi SM clock / throttle-reason samples while running."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.rows = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True,
+                                     timeout=5).stdout.strip()
+                if out:
+                    self.rows.append([c.strip() for c in out.split(",")])
+            except Exception:
+                return
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *exc):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows for k in range(4)
+                          if len(r) > 4 + k and r[4 + k].lower().startswith("active")})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def _events():
+    import torch
+    return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+def time_mode(capi, prec, steps, warmup, device, barrier=None, sampler=None):
+    """Device-resident iterations of one storage mode; returns ms per step."""
+    import torch
+    dim = WORKLOAD["dim"]
+    with capi.Lattice(dim, WORKLOAD["viscosity"], WORKLOAD["velocity"], precision=prec, stride=0,
+                      seed=WORKLOAD["seed"], noise_sigma=WORKLOAD["noise_sigma"], device=device) as L:
+        stream = torch.cuda.ExternalStream(L.stream, device=device)
+        L.step(warmup)
+        L.sync()
+        e0, e1 = _events()
+        if barrier:
+            barrier()
+        torch.cuda.synchronize(device)
+        ctx = sampler if sampler is not None else _Null()
+        with ctx:
+            e0.record(stream)
+            L.step(steps)
+            e1.record(stream)
+            e1.synchronize()
+        torch.cuda.synchronize(device)
+        if barrier:
+            barrier()
+        ms = e0.elapsed_time(e1)
+        L.sync()  # raises if the run diverged
+        return ms / steps
+
+
+class _Null:
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        return False
+
+
+def time_e2e(capi, prec, steps, device):
+    """Through the public API with host buffers: init from the host
+    configuration (lid profile copied in), `steps` iterations, and the
+    read-back of rho and u into pinned host memory, all inside the timed
+    region (host wall clock around a synchronised sequence)."""
+    import torch
+    dim = WORKLOAD["dim"]
+    n = dim ** 3
+    lid = np.full(dim * dim, WORKLOAD["velocity"])
+    mbytes = 4 if prec != "fp64" else 8
+    tdt = torch.float32 if mbytes == 4 else torch.float64
+    rho_h = torch.empty(n, dtype=tdt, pin_memory=True)
+    u_h = torch.empty(3 * n, dtype=tdt, pin_memory=True)
+    torch.cuda.synchronize(device)
+    t0 = time.perf_counter()
+    with capi.Lattice(dim, WORKLOAD["viscosity"], WORKLOAD["velocity"], precision=prec, stride=0, lid=lid,
+                      seed=WORKLOAD["seed"], noise_sigma=WORKLOAD["noise_sigma"], device=device) as L:
+        L.step(steps, every=steps)
+        L.rho(out=rho_h.numpy())
+        L.u(out=u_h.numpy())
+        L.sync()
+    t1 = time.perf_counter()
+    assert np.isfinite(rho_h.numpy()[n // 2])
+    h2d = lid.nbytes
+    d2h = rho_h.numel() * rho_h.element_size() + u_h.numel() * u_h.element_size()
+    return (t1 - t0) * 1e3, h2d, d2h
+
+
+def traffic_from_profiles(prec):
+    """DRAM bytes per launch from the committed ncu summary, scaled to 512^3."""
+    p = os.path.join(ROOT, "profiles", f"pull_{prec}.txt")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("dram_bytes_per_launch_512:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def cpu_oracle_mlups(budget_s, dim=512, threads=0):
+    """Oracle push step (FP32, all host threads) over z-slabs of a dim^3
+    lattice; returns (MLUPS, threads, description)."""
+    from oracle import pyoracle as po
+    po.build()
+    L = po.OracleLattice(dim, WORKLOAD["viscosity"], WORKLOAD["velocity"], "f32", stride=None, threads=threads)
+    nthreads = threads or po.lib().lbmo_max_threads()
+    # calibrate on 8 planes
+    t = time.perf_counter()
+    L.compute_slab(1, 9)
+    per_plane = (time.perf_counter() - t) / 8
+    planes = int(max(8, min(dim - 2, budget_s / max(per_plane, 1e-9))))
+    done, secs = 0, 0.0
+    while done < planes:
+        nz = min(planes - done, dim - 2)
+        t = time.perf_counter()
+        L.compute_slab(1, 1 + nz)
+        secs += time.perf_counter() - t
+        done += nz
+    sites = done * dim * dim
+    desc = (f"oracle C restatement of kernels.cl, FP32, OpenMP {nthreads} threads, {done} z-planes "
+            f"({sites / 1e6:.1f} M site updates) of a {dim}^3 lattice")
+    return sites / secs / 1e6, nthreads, desc, secs
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    from oracle import pyoracle as po
+    po.build()
+    dim = WORKLOAD["dim"]
+    L = po.OracleLattice(dim, WORKLOAD["viscosity"], WORKLOAD["velocity"], "f32", stride=None)
+    nthreads = po.lib().lbmo_max_threads()
+    t = time.perf_counter()
+    L.compute_slab(1, 9)
+    per_plane = (time.perf_counter() - t) / 8
+    budget = 150.0 / max(1, args.steps + args.warmup)
+    planes = int(max(1, min(dim - 2, budget / per_plane)))
+    for _ in range(args.warmup):
+        L.compute_slab(1, 1 + planes)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        L.compute_slab(1, 1 + planes)
+    secs = time.perf_counter() - t0
+    per_step_sites = planes * dim * dim
+    mlups = per_step_sites * args.steps / secs / 1e6
+    sample = (f"each step = oracle push step over {planes} z-planes ({per_step_sites / 1e6:.2f} M sites) of the "
+              f"{dim}^3 FP32 lattice, OpenMP {nthreads} threads (the reference's OpenCL CPU runtime is not "
+              f"installable here; the oracle restates kernels.cl bit-exactly)")
+    line = {"metric": METRIC, "value": round(mlups, 3), "unit": "MLUPS", "impl": "reference",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(secs * 1e3 / args.steps, 4), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"D3Q19 BGK lid-driven cavity {dim}^3 FP32 (CPU, z-slab sample)", "dim": dim,
+                       "parallelism": "host threads"},
+            "cpu_baseline": {"value": round(mlups, 3), "unit": "MLUPS", "cores": nthreads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": round(mlups, 3), "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--modes", default="fp16,bf16,fp32,fp64")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    ws, rank, local = dist_env()
+    device = local
+    torch.cuda.set_device(device)
+    barrier = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", device))
+        barrier = dist.barrier
+
+    from lbmcl_gb300 import build, capi
+    if not os.path.exists(capi.LIB_PATH):
+        build.build_library()
+    dim = WORKLOAD["dim"]
+    wet = (dim - 2) ** 3
+    peak, peak_kind = peaks()
+
+    modes = [m for m in args.modes.split(",") if m]
+    res = {}
+    sampler = ClockSampler(device)
+    for m in modes:
+        # headline mode: K steps; the others a bounded share of the run
+        k = args.steps if m == modes[0] else (max(10, args.steps // 5) if m != "fp64" else max(5, args.steps // 50))
+        ms = time_mode(capi, m, k, args.warmup if m != "fp64" else 3, device, barrier,
+                       sampler if m == modes[0] else None)
+        if ws > 1:
+            import torch.distributed as dist
+            t = torch.tensor([ms], device=f"cuda:{device}")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        mlups = wet / (ms * 1e3)
+        gbs = wet * BYTES_PER_SITE[m] / (ms * 1e-3) / 1e9
+        res[m] = {"mlups": round(mlups * ws, 1), "mlups_per_gpu": round(mlups, 1), "ms_per_step": round(ms, 4),
+                  "gbs": round(gbs, 1), "frac_hbm": round(gbs / peak, 4), "steps": k}
+
+    head = modes[0]
+    ms_head = res[head]["ms_per_step"]
+    e2e_ms, h2d, d2h = time_e2e(capi, head, args.steps, device)
+    e2e_mlups = wet * args.steps / (e2e_ms * 1e3) * ws
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        try:
+            v, cores, desc, secs = cpu_oracle_mlups(12.0)
+            cpu = {"value": round(v, 3), "unit": "MLUPS", "cores": cores, "kind": "port", "sample": desc}
+        except MemoryError:
+            v, cores, desc, secs = cpu_oracle_mlups(12.0, dim=256)
+            cpu = {"value": round(v, 3), "unit": "MLUPS", "cores": cores, "kind": "port", "sample": desc}
+
+    if rank == 0:
+        achieved = wet * BYTES_PER_SITE[head] / (ms_head * 1e-3) / 1e9
+        traffic = traffic_from_profiles(head)
+        line = {
+            "metric": METRIC, "value": res[head]["mlups"], "unit": "MLUPS", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_head, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "storage": head, "data": "synthetic",
+            "config": {"workload": (f"D3Q19 BGK lid-driven cavity {dim}^3, {head.upper()} deviation storage, "
+                                    f"FP32 arithmetic, nu={WORKLOAD['viscosity']}, lid u={WORKLOAD['velocity']}, "
+                                    f"N(0,1e-4) noise seed {WORKLOAD['seed']}"),
+                       "dim": dim, "wet_sites": wet, "l2": "inputs larger than L2 (one lattice >= 10 GB)",
+                       "parallelism": "replicas" if ws > 1 else "single GPU"},
+            "modes": res,
+            "ratio_fp16_vs_fp32": round(res["fp16"]["mlups"] / res["fp32"]["mlups"], 3)
+            if "fp16" in res and "fp32" in res else None,
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
+                         "traffic": traffic, "algorithmic_bytes_per_launch": wet * BYTES_PER_SITE[head]},
+            "e2e": {"value": round(e2e_mlups, 1), "unit": "MLUPS", "h2d_bytes_per_step": h2d / args.steps,
+                    "d2h_bytes_per_step": d2h / args.steps,
+                    "what": "lbm_init (host config + lid profile) + K iterations + rho/u read-back to pinned host"},
+            "gpu_launches": args.steps,
+            "clocks": sampler.summary(),
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

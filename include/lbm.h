@@ -1,0 +1,147 @@
+/*
+ * lbm.h -- C ABI of the GB300 (sm_103a) D3Q19 BGK lid-driven-cavity library.
+ *
+ * This is the drop-in boundary that replaces the reference's OpenCL kernel ABI
+ * and its host plumbing:
+ *   - initialize(f_stream, f_collide, density, u, map)      kernels.cl:277-282
+ *   - compute(f_stream, f_collide, density, u, map, update)  kernels.cl:321-327
+ *   - the -D macro set DIM/STRIDE/VISCOSITY/VELOCITY/FP_*     lbmcl.hpp:131-156
+ *   - buffer creation and the ping-pong enqueue loop          lbmcl.hpp:392-521
+ *   - the blocking read-backs behind the dumps                lbmcl.hpp:159-334
+ *   - OpenCL event timing                                     lbmcl.hpp:548-620
+ *
+ * Conventions
+ *   - Every function returns an lbm_status; nothing calls exit().  The text of
+ *     the last failure on the calling thread is lbm_last_error().
+ *   - A handle owns all device memory and one CUDA stream.  lbm_step is
+ *     asynchronous on that stream; lbm_dump, lbm_load, lbm_sync, lbm_timing
+ *     and lbm_reduce synchronise it.  Use one handle per host thread.
+ *   - Host buffers passed in are caller-owned; the library never keeps them.
+ *   - Iteration labels follow the reference host (lbmcl.hpp:435-520): after
+ *     lbm_step has run t iterations in total, an F dump holds the buffer that
+ *     iteration t wrote (what iteration t+1 would read), and the RHO / U
+ *     dumps hold the moments last stored, i.e. those iteration k computed
+ *     from its input when k was the last iteration with k % macro_every == 0.
+ */
+#ifndef LBM_GB300_H
+#define LBM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LBM_ABI_VERSION 1
+
+typedef struct lbm_handle lbm_t;
+
+/* Status codes. */
+typedef enum lbm_status {
+    LBM_OK = 0,
+    LBM_EINVAL = 1,    /* bad argument: dim, sizes, NULL, unknown enum        */
+    LBM_ENOMEM = 2,    /* device allocation failed or exceeds max_device_bytes */
+    LBM_ECUDA = 3,     /* a CUDA runtime call failed (no device, launch error) */
+    LBM_ESTATE = 4,    /* call not valid in the handle's current state         */
+    LBM_EDIVERGED = 5  /* a site's density became <= 0 or NaN (lbm_sync)       */
+} lbm_status;
+
+/* Population storage.  FP32/FP64 reproduce the reference's float / double
+ * builds (-F, lbm_options.hpp:214-216).  FP16/BF16 store the deviation
+ * f_i - w_i in 16 bits and do all arithmetic in FP32. */
+typedef enum lbm_precision {
+    LBM_FP32 = 0,
+    LBM_FP64 = 1,
+    LBM_FP16 = 2,
+    LBM_BF16 = 3
+} lbm_precision;
+
+/* What lbm_dump copies out / lbm_load copies in. */
+typedef enum lbm_what {
+    LBM_DUMP_F = 0,       /* populations, CSoA with the handle's stride (kernels.cl:64);
+                             float (FP32/FP16/BF16 handles) or double (FP64): dim^3*19 values */
+    LBM_DUMP_RHO = 1,     /* density, dim^3 values of the macro type                      */
+    LBM_DUMP_U = 2,       /* velocity, planar ux,uy,uz: 3*dim^3 values (kernels.cl:68-70) */
+    LBM_DUMP_MAP = 3,     /* reference cell types as int32 (common.h:7-20): dim^3 values  */
+    LBM_DUMP_MAP_U8 = 4,  /* the packed byte map the kernels read: dim^3 bytes            */
+    LBM_DUMP_F_RAW = 5    /* the raw internal population buffer (binary checkpoint)       */
+} lbm_what;
+
+typedef struct lbm_config {
+    int dim;                   /* cube edge incl. the wall layer (DIM); >= 4, multiple of 8
+                                  for FP16/BF16, of 4 otherwise                             */
+    double viscosity;          /* nu; tau = 3 nu + 0.5 (kernels.cl:61)                      */
+    double velocity;           /* lid u_x along +x (VELOCITY, kernels.cl:57)                */
+    int precision;             /* lbm_precision                                             */
+    int stride;                /* CSoA stride of F dumps (-s); power of two <= dim^3;
+                                  0 means dim^3 (pure SoA)                                  */
+    int block_threads;         /* CUDA threads per block (from -w); 0 = tuned default       */
+    uint64_t seed;             /* noise seed                                                */
+    double noise_sigma;        /* std-dev of the N(0, sigma^2) noise added to every
+                                  population of FLUID sites after initialisation; 0 = none */
+    const double *lid_profile; /* optional host array dim*dim: lid u_x of column (x,y)
+                                  at lid_profile[x + y*dim]; NULL = velocity everywhere    */
+    double tau;                /* > 0 overrides the viscosity                               */
+    size_t max_device_bytes;   /* > 0: refuse (LBM_ENOMEM) when the handle would need
+                                  more device memory than this                              */
+    int device;                /* CUDA device ordinal                                       */
+    int profile_steps;         /* 1: one CUDA event pair per iteration (reference's
+                                  per-kernel events); 0: one pair per lbm_step call         */
+} lbm_config;
+
+/* Fill *c with the reference CLI defaults (lbm_options.hpp:83-101):
+ * dim 8, nu 0.0089, u 0.05, FP32, stride 32. */
+void lbm_config_default(lbm_config *c);
+
+/* Allocate the lattice and run the initialisation kernel (replaces
+ * kernels.cl:277-318 + lbmcl.hpp:392-482, 494-498). */
+int lbm_init(lbm_t **h, const lbm_config *c);
+
+/* Enqueue nsteps iterations (replaces kernels.cl:321-425 + lbmcl.hpp:505-511).
+ * Iteration it (1-based, counted over the handle's life) stores rho and u
+ * when macro_every != 0 && it % macro_every == 0 (lbmcl.hpp:436). */
+int lbm_step(lbm_t *h, int nsteps, int macro_every);
+
+/* Copy `what` into the caller's host buffer dst of `bytes` bytes (must be
+ * exactly the size of that quantity).  Synchronous. */
+int lbm_dump(lbm_t *h, int what, void *dst, size_t bytes);
+
+/* Replace the populations by a host array in the LBM_DUMP_F layout (or
+ * LBM_DUMP_F_RAW).  The slots whose source is a wall keep the reference's
+ * fixed values.  Synchronous. */
+int lbm_load(lbm_t *h, int what, const void *src, size_t bytes);
+
+/* Byte size of `what` for this handle (0 for an unknown `what`). */
+size_t lbm_size(const lbm_t *h, int what);
+
+/* Wait for the stream; LBM_EDIVERGED once a non-finite or non-positive
+ * density has been seen by a kernel. */
+int lbm_sync(lbm_t *h);
+
+/* Elapsed times, milliseconds: total = from the initialisation kernel's start
+ * to the end of the last enqueued work (lbmcl.hpp:548-556); kernels = sum of
+ * step-kernel time (lbmcl.hpp:562-574). */
+int lbm_timing(lbm_t *h, double *total_ms, double *kernels_ms);
+
+/* Iterations run so far. */
+int lbm_iteration(const lbm_t *h, int64_t *it);
+
+/* The handle's CUDA stream (cudaStream_t), for callers that time or order
+ * their own work against it. */
+void *lbm_stream(lbm_t *h);
+
+/* FP64 sums over the sites that store macros (FLUID and MOVING) of the
+ * current state (what the next iteration would read): out[0] = mass
+ * sum(rho), out[1] = kinetic energy sum(rho |u|^2 / 2), out[2] = number of
+ * such sites.  Moments as kernels.cl:352-380 defines them.  Synchronous. */
+int lbm_reduce(lbm_t *h, double out[3]);
+
+void lbm_destroy(lbm_t *h);
+
+const char *lbm_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,499 @@
+// lbm_kernels.cuh -- the sm_103a kernels of one lattice handle.
+//
+//   pull_kernel<S, MODE>  one fused pull-stream + collide iteration
+//                         (replaces kernels.cl:321-425); MODE_REDUCE reuses
+//                         its gather to form FP64 mass / energy partials
+//   init_kernel<S>        initial state (replaces kernels.cl:277-318)
+//   dump_f_kernel<S,T>    reference post-stream buffer R_t in CSoA order
+//   load_f_kernel<S,T>    the inverse of dump_f_kernel
+//   sum_partials_kernel   deterministic final pass of the reductions
+//
+// Work decomposition of the pull kernel: one thread owns V = 16 / sizeof(S)
+// consecutive x-sites of one interior row (y, z in [1, dim-2]).  Each of the 19
+// populations is read with one aligned 16-byte load from its source row; the
+// ten populations with e_x != 0 need one more element just outside the
+// vector, read with one scalar load (the neighbouring thread's vector, so an
+// L1/L2 hit).  Results are written with one aligned 16-byte store per
+// population.  No shared memory, no shuffles in the step itself.
+#pragma once
+
+#include <string.h>
+
+#include "lbm_device.cuh"
+#include "lbm_noise.cuh"
+
+namespace lbm {
+
+template <class S> struct Compute { using type = float; };
+template <> struct Compute<double> { using type = double; };
+template <class S> __host__ __device__ constexpr bool is_dev16() { return sizeof(S) == 2; }
+
+// 16-byte vector load / store (ld.global.nc.v4 / st.global.v4).
+template <class S, int V>
+__device__ __forceinline__ void load_vec(const S *__restrict__ p, S (&out)[V])
+{
+    static_assert(V * sizeof(S) == 16, "16-byte vectors");
+    const uint4 r = __ldg(reinterpret_cast<const uint4 *>(p));
+    memcpy(out, &r, 16);
+}
+template <class S, int V>
+__device__ __forceinline__ void store_vec(S *__restrict__ p, const S (&in)[V])
+{
+    uint4 r;
+    memcpy(&r, in, 16);
+    *reinterpret_cast<uint4 *>(p) = r;
+}
+template <class S> __device__ __forceinline__ S load_one(const S *__restrict__ p)
+{
+    if constexpr (sizeof(S) == 2) {
+        const unsigned short v = __ldg(reinterpret_cast<const unsigned short *>(p));
+        S s;
+        memcpy(&s, &v, 2);
+        return s;
+    } else {
+        return __ldg(p);
+    }
+}
+template <class S> __device__ __forceinline__ S zero_elem()
+{
+    S s;
+    memset(&s, 0, sizeof(S));
+    return s;
+}
+
+// Pull one population for the V sites x0..x0+V-1 of a row: the values at
+// x - EX.  `row` points at x = 0 of the source row.
+template <class S, int V, int EX>
+__device__ __forceinline__ void gather_row(const S *__restrict__ row, int x0, int dim, S (&out)[V])
+{
+    S v[V];
+    load_vec<S, V>(row + x0, v);
+    if constexpr (EX == 0) {
+#pragma unroll
+        for (int k = 0; k < V; ++k) out[k] = v[k];
+    } else if constexpr (EX == 1) {
+        out[0] = (x0 > 0) ? load_one(row + x0 - 1) : zero_elem<S>();
+#pragma unroll
+        for (int k = 1; k < V; ++k) out[k] = v[k - 1];
+    } else {
+#pragma unroll
+        for (int k = 0; k < V - 1; ++k) out[k] = v[k + 1];
+        out[V - 1] = (x0 + V < dim) ? load_one(row + x0 + V) : zero_elem<S>();
+    }
+}
+
+template <int V> struct MapWord;
+template <> struct MapWord<2> { using type = unsigned short; };
+template <> struct MapWord<4> { using type = unsigned int; };
+template <> struct MapWord<8> { using type = unsigned long long; };
+
+template <class T> __device__ __forceinline__ T nan_of();
+template <> __device__ __forceinline__ float nan_of<float>() { return __int_as_float(0x7fc00000); }
+template <> __device__ __forceinline__ double nan_of<double>() { return __longlong_as_double(0x7ff8000000000000ll); }
+
+template <class S, int V, int I>
+__device__ __forceinline__ void gather_pop(const S *__restrict__ fin, size_t n, size_t rowoff, int dim, int x0,
+                                           S (&out)[V])
+{
+    const ptrdiff_t shift = (ptrdiff_t)ez_of(I) * dim * dim + (ptrdiff_t)ey_of(I) * dim;
+    gather_row<S, V, ex_of(I)>(fin + (size_t)I * n + rowoff - shift, x0, dim, out);
+}
+
+template <class S, int V, int I>
+__device__ __forceinline__ void gather_all(const S *__restrict__ fin, size_t n, size_t rowoff, int dim, int x0,
+                                           S (&fs)[Q][V])
+{
+    gather_pop<S, V, I>(fin, n, rowoff, dim, x0, fs[I]);
+    if constexpr (I + 1 < Q) gather_all<S, V, I + 1>(fin, n, rowoff, dim, x0, fs);
+}
+
+// ---------------------------------------------------------------------------
+// Site updates.  f holds the 19 pulled (pre-collision) values of one site.
+// ---------------------------------------------------------------------------
+struct SiteOut {
+    bool macro;      // FLUID or MOVING: stores rho/u on macro iterations
+    bool bad;        // density <= 0 or NaN on a FLUID / MOVING site
+    double r, ux, uy, uz;
+};
+
+// Exact-order FP32 / FP64 site update.  COLLIDE = false only forms moments.
+template <class T, bool COLLIDE>
+__device__ __forceinline__ void site_exact(T (&f)[Q], uint8_t b, T lidv, T inv_tau, const Weights<T> &W,
+                                           SiteOut &o)
+{
+    using O = X<T>;
+    o.macro = false;
+    o.bad = false;
+    if (b == 0) {  // FLUID
+        T r, ux, uy, uz;
+        moments_exact(f, r, ux, uy, uz);
+        o.macro = true;
+        o.bad = !(r > (T)0);
+        o.r = r; o.ux = ux; o.uy = uy; o.uz = uz;
+        if (COLLIDE) relax_exact(f, r, ux, uy, uz, inv_tau, W);
+        return;
+    }
+    if (b & M_WALL) return;
+    // sources that are walls hold the site's initial equilibrium
+#pragma unroll
+    for (int i = 0; i < Q; ++i)
+        if (wall_sourced(i, b)) f[i] = (b & M_FRONT) ? init_eq_exact(i, lidv, W) : W.w[wclass_of(i)];
+    if (b == M_FRONT) {
+        // moving lid (kernels.cl:343-349, 355, 362-367, 393-398)
+        f[5] = f[6]; f[11] = f[17]; f[12] = f[18]; f[13] = f[15]; f[14] = f[16];
+        T r = f[0];
+#pragma unroll
+        for (int i = 1; i < Q; ++i) r = O::add(r, f[i]);
+        o.macro = true;
+        o.bad = !(r > (T)0);
+        o.r = r; o.ux = lidv; o.uy = 0; o.uz = 0;
+        if (COLLIDE) {
+            const T c15 = O::mul((T)1.5, O::add(O::add(O::mul(lidv, lidv), (T)0), (T)0));
+            const T rw[3] = {O::mul(r, W.w[0]), O::mul(r, W.w[1]), O::mul(r, W.w[2])};
+#pragma unroll
+            for (int i = 0; i < Q; ++i) {
+                const T eu = ex_of(i) > 0 ? lidv : (ex_of(i) < 0 ? -lidv : (T)0);
+                f[i] = O::mul(rw[wclass_of(i)], eq_bracket_exact(eu, c15));
+            }
+        }
+        return;
+    }
+    if (b & M_CORNER) return;  // corners only propagate
+    if (COLLIDE) {
+        // full-way bounce-back of the nine opposite pairs (kernels.cl:400-408)
+        T g[Q];
+#pragma unroll
+        for (int i = 0; i < Q; ++i) g[i] = f[opp_of(i)];
+#pragma unroll
+        for (int i = 0; i < Q; ++i) f[i] = g[i];
+    }
+}
+
+// 16-bit deviation site update.  D holds s (f - w) as FP32.
+template <bool COLLIDE>
+__device__ __forceinline__ void site_dev(float (&D)[Q], uint8_t b, float lidv, float omega, float s, float inv_s,
+                                         SiteOut &o)
+{
+    o.macro = false;
+    o.bad = false;
+    if (b & M_WALL) return;
+    if (b != 0) {
+#pragma unroll
+        for (int i = 0; i < Q; ++i)
+            if (wall_sourced(i, b)) {
+                if (b & M_FRONT) {
+                    const float eu = ex_of(i) > 0 ? lidv : (ex_of(i) < 0 ? -lidv : 0.0f);
+                    D[i] = deq_scaled(i, 0.0f, 1.0f, eu, 1.5f * lidv * lidv, s);
+                } else {
+                    D[i] = 0.0f;
+                }
+            }
+    }
+    if (b == 0 || b == M_FRONT) {
+        if (b == M_FRONT) { D[5] = D[6]; D[11] = D[17]; D[12] = D[18]; D[13] = D[15]; D[14] = D[16]; }
+        float sd = 0.0f;
+#pragma unroll
+        for (int i = 0; i < Q; ++i) sd += D[i];
+        const float drho = sd * inv_s;
+        const float rho = 1.0f + drho;
+        float ux, uy, uz;
+        if (b == 0) {
+            const float jx = ((D[1] + D[7]) + (D[10] + D[11]) + D[15]) - ((D[3] + D[8]) + (D[9] + D[13]) + D[17]);
+            const float jy = ((D[2] + D[7]) + (D[8] + D[12]) + D[16]) - ((D[4] + D[9]) + (D[10] + D[14]) + D[18]);
+            const float jz = ((D[6] + D[15]) + (D[16] + D[17]) + D[18]) - ((D[5] + D[11]) + (D[12] + D[13]) + D[14]);
+            const float k = inv_s * __frcp_rn(rho);
+            ux = jx * k; uy = jy * k; uz = jz * k;
+        } else {
+            ux = lidv; uy = 0.0f; uz = 0.0f;
+        }
+        o.macro = true;
+        o.bad = !(rho > 0.0f);
+        o.r = rho; o.ux = ux; o.uy = uy; o.uz = uz;
+        if (COLLIDE) {
+            const float c15 = 1.5f * fmaf(ux, ux, fmaf(uy, uy, uz * uz));
+            if (b == 0) {
+                const float keep = 1.0f - omega;
+#pragma unroll
+                for (int i = 0; i < Q; ++i) {
+                    const float deq = deq_scaled(i, drho, rho, proj_fast(i, ux, uy, uz), c15, s);
+                    D[i] = fmaf(keep, D[i], omega * deq);
+                }
+            } else {
+#pragma unroll
+                for (int i = 0; i < Q; ++i) D[i] = deq_scaled(i, drho, rho, proj_fast(i, ux, uy, uz), c15, s);
+            }
+        }
+        return;
+    }
+    if (b & M_CORNER) return;
+    if (COLLIDE) {
+        float g[Q];
+#pragma unroll
+        for (int i = 0; i < Q; ++i) g[i] = D[opp_of(i)];
+#pragma unroll
+        for (int i = 0; i < Q; ++i) D[i] = g[i];
+    }
+}
+
+// Block reduction of (mass, energy) in double, written to partials[2*block].
+__device__ __forceinline__ void block_reduce_write(double m, double e, double *partials)
+{
+    // warp shuffles: the reductions are the only place this code uses them
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        m += __shfl_down_sync(0xffffffffu, m, off);
+        e += __shfl_down_sync(0xffffffffu, e, off);
+    }
+    __shared__ double sm[2][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) { sm[0][warp] = m; sm[1][warp] = e; }
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = (blockDim.x + 31) >> 5;
+        m = lane < nw ? sm[0][lane] : 0.0;
+        e = lane < nw ? sm[1][lane] : 0.0;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            m += __shfl_down_sync(0xffffffffu, m, off);
+            e += __shfl_down_sync(0xffffffffu, e, off);
+        }
+        if (lane == 0) {
+            partials[2 * blockIdx.x] = m;
+            partials[2 * blockIdx.x + 1] = e;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// The fused pull-stream + collide iteration.
+// ---------------------------------------------------------------------------
+template <class S, int MODE>
+__global__ void __launch_bounds__(256) pull_kernel(StepArgs a)
+{
+    constexpr int V = 16 / (int)sizeof(S);
+    using C = typename Compute<S>::type;
+    constexpr bool DEV = is_dev16<S>();
+    const unsigned g = blockIdx.x * blockDim.x + threadIdx.x;
+    double red_m = 0.0, red_e = 0.0;
+
+    if (g < a.nvec) {
+        const int dim = a.dim;
+        const unsigned xv = g % (unsigned)a.nvx;
+        const unsigned row = g / (unsigned)a.nvx;
+        const int y = 1 + (int)(row % (unsigned)(dim - 2));
+        const int z = 1 + (int)(row / (unsigned)(dim - 2));
+        const int x0 = (int)xv * V;
+        const size_t rowoff = (size_t)z * dim * dim + (size_t)y * dim;
+        const size_t site0 = rowoff + (size_t)x0;
+
+        typename MapWord<V>::type mw =
+            __ldg(reinterpret_cast<const typename MapWord<V>::type *>(a.map + site0));
+        const S *__restrict__ fin = static_cast<const S *>(a.fin);
+        S fs[Q][V];
+        gather_all<S, V, 0>(fin, a.n, rowoff, dim, x0, fs);
+
+        const bool lid_row = (z == dim - 2);
+        const C *lid = static_cast<const C *>(a.lid);
+        const Weights<C> W = make_weights<C>();
+        const C inv_tau = (C)a.inv_tau;
+        bool bad = false;
+
+#pragma unroll
+        for (int k = 0; k < V; ++k) {
+            const uint8_t b = (uint8_t)(mw >> (8 * k));
+            const C lidv = lid_row ? lid[(size_t)y * dim + x0 + k] : (C)0;
+            SiteOut o;
+            if constexpr (DEV) {
+                float D[Q];
+#pragma unroll
+                for (int i = 0; i < Q; ++i) D[i] = Dev16<S>::to_f(fs[i][k]);
+                site_dev<MODE != MODE_REDUCE>(D, b, (float)lidv, a.omega_f, Dev16<S>::scale, Dev16<S>::inv_scale, o);
+#pragma unroll
+                for (int i = 0; i < Q; ++i) fs[i][k] = Dev16<S>::from_f(D[i]);
+            } else {
+                C f[Q];
+#pragma unroll
+                for (int i = 0; i < Q; ++i) f[i] = fs[i][k];
+                site_exact<C, MODE != MODE_REDUCE>(f, b, lidv, inv_tau, W, o);
+#pragma unroll
+                for (int i = 0; i < Q; ++i) fs[i][k] = f[i];
+            }
+            bad |= o.bad;
+            if (MODE == MODE_STEP_MACRO && o.macro) {
+                C *rho = static_cast<C *>(a.rho);
+                C *u = static_cast<C *>(a.u);
+                const size_t id = site0 + k;
+                rho[id] = (C)o.r;
+                u[id] = (C)o.ux;
+                u[a.n + id] = (C)o.uy;
+                u[2 * a.n + id] = (C)o.uz;
+            }
+            if (MODE == MODE_REDUCE && o.macro) {
+                red_m += o.r;
+                red_e += 0.5 * o.r * (o.ux * o.ux + o.uy * o.uy + o.uz * o.uz);
+            }
+        }
+        if (bad) atomicOr(a.status, 1);
+
+        if (MODE != MODE_REDUCE) {
+            S *__restrict__ fout = static_cast<S *>(a.fout);
+#pragma unroll
+            for (int i = 0; i < Q; ++i) store_vec<S, V>(fout + (size_t)i * a.n + site0, fs[i]);
+        }
+    }
+    if (MODE == MODE_REDUCE) block_reduce_write(red_m, red_e, a.partials);
+}
+
+// ---------------------------------------------------------------------------
+// Initial state.  Writes P_{-1} such that S(P_{-1}) is the reference's initial
+// buffer R_0 (kernels.cl:303-317 plus the optional noise): the slot of site s
+// feeding direction i holds R_0(s + e_i)[i].  Also writes the byte map and the
+// initial rho / u (kernels.cl:290-300).
+// ---------------------------------------------------------------------------
+
+template <class C>
+__device__ __forceinline__ C lid_at(const InitArgs &a, int x, int y)
+{
+    return static_cast<const C *>(a.lid)[(size_t)y * a.dim + x];
+}
+
+template <class S>
+__global__ void init_kernel(InitArgs a)
+{
+    using C = typename Compute<S>::type;
+    const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= a.n) return;
+    const int dim = a.dim;
+    const int x = (int)(id % dim), y = (int)((id / dim) % dim), z = (int)(id / ((size_t)dim * dim));
+    const uint8_t b = pack_cell(dim, x, y, z);
+    a.map[id] = b;
+    const bool store = (b == 0) || (b == M_FRONT);
+    C *rho = static_cast<C *>(a.rho);
+    C *u = static_cast<C *>(a.u);
+    const C qn = nan_of<C>();
+    rho[id] = store ? (C)1 : qn;
+    u[id] = store ? ((b & M_FRONT) ? lid_at<C>(a, x, y) : (C)0) : qn;
+    u[a.n + id] = store ? (C)0 : qn;
+    u[2 * a.n + id] = store ? (C)0 : qn;
+
+    S *f = static_cast<S *>(a.f);
+    const Weights<C> W = make_weights<C>();
+#pragma unroll
+    for (int i = 0; i < Q; ++i) {
+        C val = qn;  // walls hold NaN (kernels.cl:312, 316)
+        if (!(b & M_WALL)) {
+            const int tx = x + ex_of(i), ty = y + ey_of(i), tz = z + ez_of(i);
+            const uint8_t tb = pack_cell(dim, tx, ty, tz);
+            if (!(tb & M_WALL)) {
+                const size_t tid = (size_t)tx + (size_t)ty * dim + (size_t)tz * dim * dim;
+                const C lv = (tb & M_FRONT) ? lid_at<C>(a, tx, ty) : (C)0;
+                if constexpr (is_dev16<S>()) {
+                    // deviation of the equilibrium at rho = 1, plus noise
+                    float d = 0.0f;
+                    if (tb & M_FRONT) {
+                        const float eu = ex_of(i) > 0 ? (float)lv : (ex_of(i) < 0 ? -(float)lv : 0.0f);
+                        d = deq_scaled(i, 0.0f, 1.0f, eu, 1.5f * (float)lv * (float)lv, 1.0f);
+                    }
+                    if (a.noise_sigma != 0.0 && tb == 0)
+                        d = d + (float)__dmul_rn(a.noise_sigma, gauss(a.seed, tid, (uint32_t)i));
+                    val = d * Dev16<S>::scale;
+                } else {
+                    val = (tb & M_FRONT) ? init_eq_exact<C>(i, lv, W) : W.w[wclass_of(i)];
+                    if (a.noise_sigma != 0.0 && tb == 0)
+                        val = X<C>::add(val, (C)__dmul_rn(a.noise_sigma, gauss(a.seed, tid, (uint32_t)i)));
+                }
+            }
+        }
+        if constexpr (is_dev16<S>()) {
+            f[(size_t)i * a.n + id] = Dev16<S>::from_f((float)val);
+        } else {
+            f[(size_t)i * a.n + id] = (S)val;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Dump / load of the reference's post-stream buffer R_t in CSoA order.
+// Output element o <-> (site id, q): o = (((id >> sd) * 19 + q) << sd) + (id & (2^sd - 1))
+// (kernels.cl:64).  Chunked by output index so any stride works.
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ void decode_csoa(size_t o, int sd, size_t n, size_t &id, int &q)
+{
+    if (sd < 0) {  // pure SoA of a non-power-of-two lattice: o = q * n + id
+        q = (int)(o / n);
+        id = o - (size_t)q * n;
+        return;
+    }
+    const size_t smask = ((size_t)1 << sd) - 1;
+    const size_t lane = o & smask;
+    const size_t t = o >> sd;
+    q = (int)(t % Q);
+    id = ((t / Q) << sd) | lane;
+}
+
+template <class S, class C>
+__device__ __forceinline__ C stored_value(const S *f, size_t n, int q, size_t src)
+{
+    const S v = f[(size_t)q * n + src];
+    if constexpr (is_dev16<S>()) {
+        return (C)(wf_of(q) + Dev16<S>::to_f(v) * Dev16<S>::inv_scale);
+    } else {
+        return (C)v;
+    }
+}
+
+template <class S, class T>
+__global__ void dump_f_kernel(DumpArgs a)
+{
+    using C = typename Compute<S>::type;
+    const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= a.count) return;
+    size_t id;
+    int q;
+    decode_csoa(a.o0 + k, a.sd, a.n, id, q);
+    const int dim = a.dim;
+    const int x = (int)(id % dim), y = (int)((id / dim) % dim), z = (int)(id / ((size_t)dim * dim));
+    const uint8_t b = a.map[id];
+    const int sx = x - ex_of(q), sy = y - ey_of(q), sz = z - ez_of(q);
+    const bool in = sx >= 0 && sy >= 0 && sz >= 0 && sx < dim && sy < dim && sz < dim;
+    const size_t src = in ? (size_t)sx + (size_t)sy * dim + (size_t)sz * dim * dim : 0;
+    const bool src_wall = !in || (a.map[src] & M_WALL);
+    const S *f = static_cast<const S *>(a.f);
+    T val;
+    if (b & M_WALL) {
+        val = src_wall ? (T)nan_of<C>() : (T)stored_value<S, C>(f, a.n, q, src);
+    } else if (src_wall) {
+        const Weights<C> W = make_weights<C>();
+        C lv = (b & M_FRONT) ? static_cast<const C *>(a.lid)[(size_t)y * dim + x] : (C)0;
+        val = (T)((b & M_FRONT) ? init_eq_exact<C>(q, lv, W) : W.w[wclass_of(q)]);
+    } else {
+        val = (T)stored_value<S, C>(f, a.n, q, src);
+    }
+    static_cast<T *>(a.buf)[k] = val;
+}
+
+template <class S, class T>
+__global__ void load_f_kernel(DumpArgs a)
+{
+    const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= a.count) return;
+    size_t id;
+    int q;
+    decode_csoa(a.o0 + k, a.sd, a.n, id, q);
+    const int dim = a.dim;
+    const int x = (int)(id % dim), y = (int)((id / dim) % dim), z = (int)(id / ((size_t)dim * dim));
+    const int sx = x - ex_of(q), sy = y - ey_of(q), sz = z - ez_of(q);
+    if (sx < 0 || sy < 0 || sz < 0 || sx >= dim || sy >= dim || sz >= dim) return;
+    const size_t src = (size_t)sx + (size_t)sy * dim + (size_t)sz * dim * dim;
+    if (a.map[src] & M_WALL) return;
+    const T v = static_cast<const T *>(a.buf)[k];
+    S *f = static_cast<S *>(a.f);
+    if constexpr (is_dev16<S>()) {
+        f[(size_t)q * a.n + src] = Dev16<S>::from_f(((float)v - wf_of(q)) * Dev16<S>::scale);
+    } else {
+        f[(size_t)q * a.n + src] = (S)v;
+    }
+}
+
+}  // namespace lbm

@@ -1,0 +1,30 @@
+// lbm_launch.h -- host-side launchers of the kernels, one translation unit
+// per storage type (lbm_kernels_<type>.cu) so they compile in parallel.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "lbm_device.cuh"
+
+namespace lbm {
+
+struct InitArgs;
+struct DumpArgs;
+
+// prec: 0 FP32, 1 FP64, 2 FP16, 3 BF16 (lbm_precision)
+#define LBM_DECLARE_LAUNCHERS(SFX)                                                                   \
+    cudaError_t launch_pull_##SFX(int mode, const StepArgs &a, unsigned grid, unsigned block,        \
+                                  cudaStream_t s);                                                   \
+    cudaError_t launch_init_##SFX(const InitArgs &a, cudaStream_t s);                               \
+    cudaError_t launch_dump_##SFX(const DumpArgs &a, cudaStream_t s);                               \
+    cudaError_t launch_load_##SFX(const DumpArgs &a, cudaStream_t s);                               \
+    const void *pull_kernel_ptr_##SFX(int mode);
+
+LBM_DECLARE_LAUNCHERS(f32)
+LBM_DECLARE_LAUNCHERS(f64)
+LBM_DECLARE_LAUNCHERS(f16)
+LBM_DECLARE_LAUNCHERS(bf16)
+
+cudaError_t launch_sum_partials(const double *partials, int nblocks, double *out, cudaStream_t s);
+
+}  // namespace lbm

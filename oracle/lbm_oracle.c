@@ -1,0 +1,166 @@
+/*
+ * lbm_oracle.c -- CPU oracle for LBMCL's D3Q19 BGK lid-driven-cavity step.
+ *
+ * TEST INFRASTRUCTURE ONLY (see lbm_oracle.h): the checker for the CUDA
+ * library and the timed CPU baseline, never part of the product path.
+ */
+#include "lbm_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define LBMO_Q 19
+
+/* D3Q19 velocity set in the reference's ordering (kernels.cl:131-205):
+ * 0 rest; 1..6 = +x,+y,-x,-y,-z,+z; 7..18 the edge directions. */
+static const int LBMO_EX[LBMO_Q] = {0, 1, 0, -1, 0, 0, 0, 1, -1, -1, 1, 1, 0, -1, 0, 1, 0, -1, 0};
+static const int LBMO_EY[LBMO_Q] = {0, 0, 1, 0, -1, 0, 0, 1, 1, -1, -1, 0, 1, 0, -1, 0, 1, 0, -1};
+static const int LBMO_EZ[LBMO_Q] = {0, 0, 0, 0, 0, -1, 1, 0, 0, 0, 0, -1, -1, -1, -1, 1, 1, 1, 1};
+/* opposite direction S_i (kernels.cl:208-226) */
+static const int LBMO_OPP[LBMO_Q] = {0, 3, 4, 1, 2, 6, 5, 9, 10, 7, 8, 17, 18, 15, 16, 13, 14, 11, 12};
+
+/* Cell-type predicates (common.h:23-66). */
+static inline int lbmo_is_moving_init(int ct) { return ct & LBMO_FRONT; }
+static inline int lbmo_is_fluid(int ct) { return ct == LBMO_FLUID; }
+static inline int lbmo_is_wall(int ct) { return ct == LBMO_WALL; }
+static inline int lbmo_is_boundary(int ct)
+{
+    return ct & (LBMO_LEFT | LBMO_RIGHT | LBMO_BOTTOM | LBMO_TOP | LBMO_BACK | LBMO_FRONT);
+}
+static inline int lbmo_is_moving(int ct) { return ct & LBMO_MOVING; }
+static inline int lbmo_is_store_macro(int ct) { return lbmo_is_fluid(ct) || lbmo_is_moving(ct); }
+static inline int lbmo_is_collision(int ct) { return lbmo_is_fluid(ct) || lbmo_is_moving(ct); }
+static inline int lbmo_is_bounceback(int ct) { return lbmo_is_boundary(ct) && !(ct & LBMO_MOVING); }
+
+int lbmo_max_threads(void)
+{
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+static double lbmo_now(void)
+{
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
+
+/* kernels.cl:236-266: face flags on the first interior layer, WALL on the
+ * outer layer, CORNER for the four BACK corners, MOVING on the bare FRONT face,
+ * FLUID elsewhere. */
+int lbmo_cell_type(int dim, int x, int y, int z)
+{
+    int ct = LBMO_NONE;
+    if (x == 1) ct |= LBMO_LEFT;
+    if (x == dim - 2) ct |= LBMO_RIGHT;
+    if (y == 1) ct |= LBMO_BOTTOM;
+    if (y == dim - 2) ct |= LBMO_TOP;
+    if (z == 1) ct |= LBMO_BACK;
+    if (z == dim - 2) ct |= LBMO_FRONT;
+    if (x == 0 || x == dim - 1 || y == 0 || y == dim - 1 || z == 0 || z == dim - 1) ct = LBMO_WALL;
+    if (ct == (LBMO_LEFT | LBMO_BACK | LBMO_BOTTOM) || ct == (LBMO_RIGHT | LBMO_BACK | LBMO_BOTTOM) ||
+        ct == (LBMO_LEFT | LBMO_BACK | LBMO_TOP) || ct == (LBMO_RIGHT | LBMO_BACK | LBMO_TOP))
+        ct = LBMO_CORNER;
+    if (ct == LBMO_FRONT) ct |= LBMO_MOVING;
+    if (ct == LBMO_NONE) ct = LBMO_FLUID;
+    return ct;
+}
+
+/* ---------------------------------------------------------------------------
+ * Seeded noise.  Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random
+ * numbers: as easy as 1, 2, 3", SC'11): 10 rounds of two 32x32->64
+ * multiplications with the published multipliers and Weyl key increments.
+ * ------------------------------------------------------------------------- */
+void lbmo_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4])
+{
+    uint32_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3];
+    uint32_t k0 = key[0], k1 = key[1];
+    for (int r = 0; r < 10; ++r) {
+        const uint64_t p0 = (uint64_t)0xD2511F53u * c0;
+        const uint64_t p1 = (uint64_t)0xCD9E8D57u * c2;
+        const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ k0;
+        const uint32_t n1 = (uint32_t)p1;
+        const uint32_t n2 = (uint32_t)(p0 >> 32) ^ c3 ^ k1;
+        const uint32_t n3 = (uint32_t)p0;
+        c0 = n0; c1 = n1; c2 = n2; c3 = n3;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+/* ln(x) for finite x > 0: x = m 2^e with m in [sqrt(1/2), sqrt(2)), then
+ * ln m = 2 atanh(s), s = (m-1)/(m+1), summed as the odd series
+ * 2 s (1 + s^2/3 + s^4/5 + ... + s^22/23) (|s| <= 0.1716, so the truncation
+ * error is below 1e-18).  Uses only IEEE + - * /, no library call. */
+double lbmo_log(double x)
+{
+    uint64_t bits;
+    memcpy(&bits, &x, sizeof bits);
+    int e = (int)((bits >> 52) & 0x7ff);
+    if (e == 0) { /* subnormal: scale by 2^54 exactly */
+        x = x * 18014398509481984.0;
+        memcpy(&bits, &x, sizeof bits);
+        e = (int)((bits >> 52) & 0x7ff) - 54;
+    }
+    e -= 1023;
+    bits = (bits & 0x000fffffffffffffull) | 0x3ff0000000000000ull; /* m in [1,2) */
+    double m;
+    memcpy(&m, &bits, sizeof m);
+    if (m > 1.4142135623730951) { m = m * 0.5; e += 1; }
+    const double s = (m - 1.0) / (m + 1.0);
+    const double s2 = s * s;
+    double acc = 1.0 / 23.0;
+    for (int k = 10; k >= 0; --k) acc = (1.0 / (double)(2 * k + 1)) + s2 * acc;
+    /* the loop above starts at 1/23 and folds 1/21 .. 1/1 in: acc = sum s2^k/(2k+1) */
+    const double ln2 = 0.6931471805599453;
+    return ((double)e * ln2) + ((2.0 * s) * acc);
+}
+
+/* Uniform in (-1, 1) from two 32-bit words (53 random bits). */
+static inline double lbmo_sym_uniform(uint32_t a, uint32_t b)
+{
+    const uint64_t m = ((uint64_t)(a >> 5) << 26) | (uint64_t)(b >> 6);
+    const double u01 = ((double)m + 0.5) * (1.0 / 9007199254740992.0);
+    return (2.0 * u01) - 1.0;
+}
+
+/* Standard normal by the Marsaglia polar method on the counter stream
+ * (site, q, attempt); attempt is bounded, so the loop always ends. */
+double lbmo_gauss(uint64_t seed, uint64_t site, uint32_t q)
+{
+    const uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+    for (uint32_t attempt = 0; attempt < 64; ++attempt) {
+        const uint32_t ctr[4] = {(uint32_t)site, (uint32_t)(site >> 32), q, attempt};
+        uint32_t r[4];
+        lbmo_philox4x32_10(ctr, key, r);
+        const double v1 = lbmo_sym_uniform(r[0], r[1]);
+        const double v2 = lbmo_sym_uniform(r[2], r[3]);
+        const double s = (v1 * v1) + (v2 * v2);
+        if (s >= 1.0 || s == 0.0) continue;
+        const double t = (-2.0 * lbmo_log(s)) / s;
+        return v1 * sqrt(t);
+    }
+    return 0.0;
+}
+
+/* ---- precision-generic body, instantiated for float and double ---------- */
+#define REAL float
+#define SFX(name) name##_f32
+#include "lbm_oracle_body.h"
+#undef REAL
+#undef SFX
+
+#define REAL double
+#define SFX(name) name##_f64
+#include "lbm_oracle_body.h"
+#undef REAL
+#undef SFX

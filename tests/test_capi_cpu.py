@@ -1,0 +1,82 @@
+"""The C-ABI library without a GPU: it loads, exports every function
+include/lbm.h declares, and rejects bad arguments before touching CUDA."""
+import ctypes as C
+import subprocess
+
+import pytest
+
+
+def test_exports_every_declared_symbol(libonly):
+    names = libonly.declared_functions()
+    assert {"lbm_init", "lbm_step", "lbm_dump", "lbm_destroy", "lbm_last_error"} <= set(names)
+    L = libonly.lib()
+    for n in names:
+        assert hasattr(L, n), f"{n} declared in include/lbm.h but not exported"
+    out = subprocess.run(["nm", "-D", "--defined-only", libonly.LIB_PATH], capture_output=True, text=True).stdout
+    exported = {line.split()[-1] for line in out.splitlines() if " T " in line}
+    missing = [n for n in names if n not in exported]
+    assert not missing, missing
+
+
+def test_config_defaults_are_the_reference_cli_defaults(libonly):
+    c = libonly.default_config()
+    # lbm_options.hpp:83-101
+    assert (c.dim, c.viscosity, c.velocity, c.precision, c.stride) == (8, 0.0089, 0.05, libonly.FP32, 32)
+    assert c.noise_sigma == 0.0 and c.block_threads == 0 and not c.lid_profile
+
+
+def _init(libonly, **kw):
+    c = libonly.default_config()
+    for k, v in kw.items():
+        setattr(c, k, v)
+    h = C.c_void_p()
+    rc = libonly.lib().lbm_init(C.byref(h), C.byref(c))
+    return rc, libonly.lib().lbm_last_error().decode()
+
+
+@pytest.mark.parametrize("kw,frag", [
+    (dict(dim=3), "dim"),
+    (dict(dim=10), "multiple of 4"),
+    (dict(dim=12, precision=2), "multiple of 8"),
+    (dict(dim=4096), "dim"),
+    (dict(precision=7), "precision"),
+    (dict(stride=24), "stride"),
+    (dict(stride=1024), "stride"),       # > dim^3 = 512
+    (dict(stride=-1), "stride"),
+    (dict(dim=12, stride=1024), "stride"),  # does not divide 1728
+    (dict(viscosity=-1.0), "viscosity"),
+    (dict(velocity=float("inf")), "velocity"),
+    (dict(noise_sigma=-1.0), "noise"),
+    (dict(block_threads=4096), "block_threads"),
+])
+def test_init_rejects_bad_arguments(libonly, kw, frag):
+    rc, msg = _init(libonly, **kw)
+    assert rc == libonly.EINVAL
+    assert frag in msg
+
+
+def test_init_respects_device_budget(libonly):
+    # fault injection on the host: an allocation that would exceed the
+    # configured budget fails cleanly with ENOMEM before any CUDA call
+    rc, msg = _init(libonly, dim=64, max_device_bytes=1 << 20)
+    assert rc == libonly.ENOMEM
+    assert "budget" in msg
+
+
+def test_null_arguments(libonly):
+    L = libonly.lib()
+    assert L.lbm_init(None, None) == libonly.EINVAL
+    assert L.lbm_step(None, 1, 0) == libonly.EINVAL
+    assert L.lbm_dump(None, 0, None, 0) == libonly.EINVAL
+    assert L.lbm_sync(None) == libonly.EINVAL
+    assert L.lbm_size(None, 0) == 0
+    assert L.lbm_stream(None) is None
+    L.lbm_destroy(None)
+
+
+def test_lid_profile_must_be_finite(libonly):
+    import numpy as np
+    lid = np.full(64, 0.05)
+    lid[7] = np.nan
+    rc, msg = _init(libonly, lid_profile=lid.ctypes.data_as(C.POINTER(C.c_double)))
+    assert rc == libonly.EINVAL and "lid_profile" in msg

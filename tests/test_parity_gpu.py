@@ -1,0 +1,210 @@
+"""Parity of the sm_103a library (through the C ABI) with the CPU oracle.
+
+Bars (the benchmark spec): max |df| <= 1e-5 in FP32 and <= 1e-12 in FP64 against the
+oracle on identical inputs, lattice map bit-exact.  The FP32 / FP64 kernels
+evaluate every expression in the reference's operand order without FMA
+contraction, so they are also checked for bit-for-bit equality.
+"""
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+TOL = {"f32": 1e-5, "f64": 1e-12}
+GPU_PREC = {"f32": "fp32", "f64": "fp64"}
+
+
+def assert_f_close(gpu, ref, tol, what=""):
+    assert gpu.shape == ref.shape
+    gn, rn = np.isnan(gpu), np.isnan(ref)
+    assert np.array_equal(gn, rn), f"{what}: NaN positions differ ({(gn != rn).sum()} slots)"
+    d = np.abs(gpu[~gn].astype(np.float64) - ref[~rn].astype(np.float64))
+    assert d.size == 0 or d.max() <= tol, f"{what}: max |df| = {d.max():.3e} > {tol}"
+
+
+def bits(a):
+    return a.view(np.uint32 if a.dtype == np.float32 else np.uint64)
+
+
+@pytest.mark.parametrize("dim", [4, 8, 12, 16, 32])
+def test_map_bit_exact(capi, oracle, dim):
+    with capi.Lattice(dim, precision="fp32", stride=0) as L:
+        np.testing.assert_array_equal(L.cell_map(), oracle.cell_types(dim))
+
+
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+@pytest.mark.parametrize("dim,stride", [(8, 8), (32, 8), (16, 1), (16, 4096), (4, 4), (12, 16)])
+def test_f_after_each_step(capi, oracle, prec, dim, stride):
+    """Config 1 shape (32^3, stride 8, 10 steps) and layout / size variations:
+    the full post-stream buffer, wall slots included, after every iteration."""
+    o = oracle.OracleLattice(dim, 0.0089, 0.05, prec, stride)
+    with capi.Lattice(dim, 0.0089, 0.05, precision=GPU_PREC[prec], stride=stride) as L:
+        assert_f_close(L.f(), o.state, TOL[prec], "initial")
+        for it in range(1, 11):
+            o.step(1, every=1)
+            L.step(1, every=1)
+            g = L.f()
+            assert_f_close(g, o.state, TOL[prec], f"iteration {it}")
+            assert np.array_equal(bits(g), bits(o.state)), f"iteration {it}: not bit-identical"
+            np.testing.assert_array_equal(bits(L.rho()), bits(o.rho))
+            np.testing.assert_array_equal(bits(L.u()), bits(o.u))
+
+
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+def test_lid_profile_noise_and_macro_every(capi, oracle, prec):
+    """Per-column lid, seeded noise on FLUID populations, macros every 3rd
+    iteration; 60 iterations at 24^3 with block-size and stride changes."""
+    rng = np.random.default_rng(11)
+    dim = 24
+    lid = 0.05 + 0.01 * rng.standard_normal(dim * dim)
+    o = oracle.OracleLattice(dim, 0.01, 0.05, prec, 64, lid=lid, seed=1234, noise_sigma=1e-4)
+    with capi.Lattice(dim, 0.01, 0.05, precision=GPU_PREC[prec], stride=64, lid=lid, seed=1234,
+                      noise_sigma=1e-4, block_threads=96) as L:
+        assert np.array_equal(bits(L.f()), bits(o.state)), "initial state (noise) differs"
+        for chunk in (1, 2, 7, 20, 30):
+            o.step(chunk, every=3)
+            L.step(chunk, every=3)
+            g = L.f()
+            assert_f_close(g, o.state, TOL[prec], f"after {o.it}")
+            assert np.array_equal(bits(g), bits(o.state))
+            np.testing.assert_array_equal(bits(L.rho()), bits(o.rho))
+            np.testing.assert_array_equal(bits(L.u()), bits(o.u))
+        assert L.iteration == o.it == 60
+
+
+def test_golden_sailfish_8_and_32(capi):
+    """make test8 / make test32 through the library against the reference's
+    golden data (verify.py metrics)."""
+    from lbmcl_gb300 import vti
+    g8 = np.load(os.path.join(GOLD, "sailfish_ldc8.npz"))
+    with capi.Lattice(8, precision="fp32", stride=8) as L:
+        for it in range(0, 11):
+            if it:
+                L.step(1, every=1)
+            c = vti.compare({"rho": g8[f"rho_{it}"], "v": g8[f"v_{it}"]}, vti.interior_fields(8, L.rho(), L.u()))
+            assert c["mae_rho"] < 2e-6 and c["mae_v"] < 1e-6, (it, c)
+    g32 = np.load(os.path.join(GOLD, "sailfish_ldc32.npz"))
+    with capi.Lattice(32, precision="fp32", stride=32) as L:
+        done = 0
+        for it in (20, 500):
+            L.step(it - done, every=20)
+            done = it
+            c = vti.compare({"rho": g32[f"rho_{it}"], "v": g32[f"v_{it}"]}, vti.interior_fields(32, L.rho(), L.u()))
+            assert c["mae_rho"] < 5e-6 and c["mae_v"] < 2e-6, (it, c)
+
+
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+def test_64cube_200_steps(capi, oracle, prec):
+    o = oracle.OracleLattice(64, 0.0089, 0.05, prec, 64, seed=7, noise_sigma=1e-4)
+    with capi.Lattice(64, 0.0089, 0.05, precision=GPU_PREC[prec], stride=64, seed=7, noise_sigma=1e-4) as L:
+        o.step(200, every=100)
+        L.step(200, every=100)
+        g = L.f()
+        assert_f_close(g, o.state, TOL[prec], "64^3 x 200")
+        assert np.array_equal(bits(g), bits(o.state))
+
+
+@pytest.mark.parametrize("prec", ["fp32", "fp64", "fp16", "bf16"])
+def test_load_dump_round_trip(capi, prec):
+    with capi.Lattice(16, precision=prec, stride=16, seed=3, noise_sigma=1e-4) as L:
+        L.step(5)
+        f0 = L.f()
+        raw = L.raw()
+        L.load_f(f0)
+        f1 = L.f()
+        np.testing.assert_array_equal(np.isnan(f0), np.isnan(f1))
+        if prec in ("fp32", "fp64"):
+            np.testing.assert_array_equal(bits(f0), bits(f1))
+        else:
+            assert np.nanmax(np.abs(f1 - f0)) < 1e-6
+        L.load_raw(raw)
+        np.testing.assert_array_equal(L.raw(), raw)
+
+
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+def test_load_then_continue(capi, oracle, prec):
+    """A state loaded from the host continues exactly like the oracle."""
+    o = oracle.OracleLattice(16, 0.0089, 0.05, prec, 8, seed=5, noise_sigma=1e-4)
+    o.step(7, every=0)
+    with capi.Lattice(16, 0.0089, 0.05, precision=GPU_PREC[prec], stride=8) as L:
+        L.load_f(o.state)
+        assert np.array_equal(bits(L.f()), bits(o.state))
+        o.step(5, every=5)
+        L.step(5, every=5)
+        assert np.array_equal(bits(L.f()), bits(o.state))
+
+
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+def test_reduce_matches_oracle_moments(capi, oracle, prec):
+    dim = 32
+    o = oracle.OracleLattice(dim, 0.0089, 0.05, prec, 32, seed=1, noise_sigma=1e-4)
+    with capi.Lattice(dim, 0.0089, 0.05, precision=GPU_PREC[prec], stride=32, seed=1, noise_sigma=1e-4) as L:
+        o.step(25, every=0)
+        L.step(25, every=0)
+        mass, energy, count = L.reduce()
+    # the moments of the current state are what the next iteration stores
+    o.step(1, every=1)
+    sm = (o.map == oracle.FLUID) | ((o.map & oracle.MOVING) != 0)
+    r = o.rho[sm].astype(np.float64)
+    u = o.u.reshape(3, -1)[:, sm].astype(np.float64)
+    m_ref = r.sum()
+    e_ref = (0.5 * r * (u ** 2).sum(0)).sum()
+    assert count == sm.sum()
+    assert abs(mass - m_ref) <= 1e-12 * m_ref
+    assert abs(energy - e_ref) <= 1e-9 * e_ref
+
+
+def test_sixteen_bit_storage_close_to_fp64(capi):
+    """FP16 / BF16 deviation storage against the FP64 run, same seed."""
+    dim, steps = 32, 300
+    kw = dict(viscosity=0.005, velocity=0.08, stride=32, seed=9, noise_sigma=1e-4)
+    with capi.Lattice(dim, precision="fp64", **kw) as R:
+        R.step(steps, every=steps)
+        u64 = R.u().reshape(3, dim, dim, dim)
+        r64 = R.rho()
+    errs = {}
+    for prec in ("fp16", "bf16", "fp32"):
+        with capi.Lattice(dim, precision=prec, **kw) as L:
+            L.step(steps, every=steps)
+            u = L.u().reshape(3, dim, dim, dim).astype(np.float64)
+            r = L.rho().astype(np.float64)
+        fluid = ~np.isnan(u64[0])
+        mid = u64[0, :, dim // 2, :]
+        e_mid = np.linalg.norm(np.nan_to_num(u[0, :, dim // 2, :] - mid)) / np.linalg.norm(np.nan_to_num(mid))
+        e_rho = np.nanmax(np.abs(r - r64))
+        errs[prec] = (e_mid, e_rho)
+        assert np.isfinite(u[:, fluid]).all()
+    assert errs["fp32"][0] < 1e-5
+    assert errs["fp16"][0] < 1e-3, errs
+    assert errs["bf16"][0] < 2e-2, errs
+
+
+def test_divergence_is_reported(capi):
+    """An unstable run (tau near 0.5, lid near the lattice sound speed) makes
+    densities non-finite; lbm_sync reports it as EDIVERGED."""
+    with capi.Lattice(16, viscosity=0.0, velocity=0.6, precision="fp32") as L:
+        L.step(400)
+        with pytest.raises(capi.LbmError) as e:
+            L.sync()
+        assert e.value.code == capi.EDIVERGED
+
+
+def test_timing_and_iteration_counters(capi):
+    with capi.Lattice(32, precision="fp32", profile_steps=True) as L:
+        L.step(10)
+        L.step(5, every=5)
+        tot, ker = L.timing()
+        assert L.iteration == 15
+        assert tot > 0 and 0 < ker <= tot
+
+
+def test_deterministic_repeat(capi):
+    outs = []
+    for _ in range(2):
+        with capi.Lattice(48, precision="fp16", seed=4, noise_sigma=1e-4) as L:
+            L.step(40)
+            outs.append(L.raw())
+    np.testing.assert_array_equal(outs[0], outs[1])
