@@ -1,0 +1,42 @@
+"""Run one cavity through the C ABI and report MLUPS (also the small case
+the ncu captures profile).
+
+    python -m lbmcl_gb300.run --dim 256 --precision fp16 --steps 4 [--every 0]
+"""
+from __future__ import annotations
+
+import argparse
+import time
+
+from . import capi
+
+
+def main(argv=None) -> int:
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--dim", type=int, default=256)
+    ap.add_argument("--precision", default="fp32", choices=sorted(capi.PRECISIONS))
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--every", type=int, default=0)
+    ap.add_argument("--viscosity", type=float, default=0.0089)
+    ap.add_argument("--velocity", type=float, default=0.05)
+    ap.add_argument("--noise", type=float, default=1e-4)
+    ap.add_argument("--seed", type=int, default=1234)
+    ap.add_argument("--block", type=int, default=0)
+    a = ap.parse_args(argv)
+    with capi.Lattice(a.dim, a.viscosity, a.velocity, precision=a.precision, stride=0, seed=a.seed,
+                      noise_sigma=a.noise, block_threads=a.block, profile_steps=True) as L:
+        t0 = time.perf_counter()
+        L.step(a.steps, every=a.every)
+        L.sync()
+        wall = time.perf_counter() - t0
+        total_ms, kernels_ms = L.timing()
+        mass, energy, count = L.reduce()
+    wet = (a.dim - 2) ** 3
+    print(f"dim={a.dim} precision={a.precision} steps={a.steps} kernels={kernels_ms:.3f} ms "
+          f"kernel MLUPS={wet * a.steps / (kernels_ms * 1e3):.1f} wall={wall * 1e3:.1f} ms "
+          f"mass={mass:.9e} energy={energy:.6e} sites={count:.0f}")
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())
