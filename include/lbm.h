@@ -88,7 +88,17 @@ typedef struct lbm_config {
     int device;                /* CUDA device ordinal                                       */
     int profile_steps;         /* 1: one CUDA event pair per iteration (reference's
                                   per-kernel events); 0: one pair per lbm_step call         */
+    int kernel;                /* lbm_kernel: iteration kernel variant; 0 = tuned default  */
+    int stages;                /* TMA-staged kernel: pipeline depth (0 = tuned default)    */
 } lbm_config;
+
+/* Iteration kernel variants (same results, different data movement). */
+typedef enum lbm_kernel {
+    LBM_KERNEL_AUTO = 0,
+    LBM_KERNEL_DIRECT = 1,   /* per-thread 16-byte vector loads straight from HBM        */
+    LBM_KERNEL_STAGED = 2    /* persistent CTAs; whole source rows staged in shared
+                                memory by cp.async.bulk (TMA) through an mbarrier ring   */
+} lbm_kernel;
 
 /* Fill *c with the reference CLI defaults (lbm_options.hpp:83-101):
  * dim 8, nu 0.0089, u 0.05, FP32, stride 32. */

@@ -18,6 +18,7 @@ HEADER = os.path.join(os.path.dirname(PKG), "include", "lbm.h")
 
 FP32, FP64, FP16, BF16 = 0, 1, 2, 3
 PRECISIONS = {"fp32": FP32, "fp64": FP64, "fp16": FP16, "bf16": BF16}
+KERNELS = {"auto": 0, "direct": 1, "staged": 2}
 DUMP_F, DUMP_RHO, DUMP_U, DUMP_MAP, DUMP_MAP_U8, DUMP_F_RAW = 0, 1, 2, 3, 4, 5
 OK, EINVAL, ENOMEM, ECUDA, ESTATE, EDIVERGED = 0, 1, 2, 3, 4, 5
 Q = 19
@@ -44,6 +45,8 @@ class Config(C.Structure):
         ("max_device_bytes", C.c_size_t),
         ("device", C.c_int),
         ("profile_steps", C.c_int),
+        ("kernel", C.c_int),
+        ("stages", C.c_int),
     ]
 
 
@@ -112,7 +115,7 @@ class Lattice:
 
     def __init__(self, dim, viscosity=0.0089, velocity=0.05, precision="fp32", stride=None, lid=None,
                  seed=0, noise_sigma=0.0, tau=0.0, block_threads=0, max_device_bytes=0, device=0,
-                 profile_steps=False):
+                 profile_steps=False, kernel=0, stages=0):
         L = lib()
         c = default_config()
         c.dim = int(dim)
@@ -131,6 +134,8 @@ class Lattice:
         c.max_device_bytes = int(max_device_bytes)
         c.device = int(device)
         c.profile_steps = 1 if profile_steps else 0
+        c.kernel = KERNELS[kernel] if isinstance(kernel, str) else int(kernel)
+        c.stages = int(stages)
         self.cfg = c
         self.dim = int(dim)
         self.n = self.dim ** 3

@@ -115,6 +115,11 @@ struct lbm_handle {
     unsigned block = 128;
     unsigned nvec = 0;
     unsigned grid = 0;
+    // staged variant (LBM_KERNEL_STAGED)
+    int kernel = LBM_KERNEL_DIRECT;
+    int rows = 1, gpp = 0, stages = 0;
+    unsigned ngroups = 0, sgrid = 0, sblock = 0;
+    size_t ssmem = 0;
 };
 
 namespace {
@@ -187,11 +192,72 @@ lbm::StepArgs step_args(const lbm_t *h, int from)
     a.n = h->n;
     a.inv_tau = h->inv_tau;
     a.omega_f = h->omega_f;
+    a.rows = h->rows;
+    a.gpp = h->gpp;
+    a.ngroups = h->ngroups;
+    a.stages = h->stages;
     return a;
+}
+
+const void *staged_ptr(int prec, int mode)
+{
+    switch (prec) {
+    case LBM_FP32: return lbm::staged_kernel_ptr_f32(mode);
+    case LBM_FP64: return lbm::staged_kernel_ptr_f64(mode);
+    case LBM_FP16: return lbm::staged_kernel_ptr_f16(mode);
+    default: return lbm::staged_kernel_ptr_bf16(mode);
+    }
+}
+
+// Shape the staged variant: rows per group, ring depth, threads, persistent
+// grid.  Returns false when the ring does not fit (the direct variant is used).
+int setup_staged(lbm_t *h, int want_stages)
+{
+    const int dim = h->dim;
+    const size_t sb = storage_bytes(h->prec);
+    const int V = 4;
+    const int nvx = dim / V;
+    int rows = std::max(1, 512 / dim);
+    rows = std::min(rows, dim - 2);
+    const size_t stage_bytes = (size_t)lbm::Q * rows * dim * sb;
+    int dev = 0, smem_optin = 0, nsm = 0;
+    LBM_CUDA(cudaGetDevice(&dev));
+    LBM_CUDA(cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    LBM_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    const size_t cap = (size_t)smem_optin - 128;
+    int stages = want_stages > 0 ? want_stages : (int)std::min<size_t>(8, std::max<size_t>(2, (110u << 10) / stage_bytes));
+    while (stages > 2 && 128 + stages * stage_bytes > cap) --stages;
+    if (stages < 2 || 128 + stages * stage_bytes > cap) return fail(LBM_EINVAL, "staged kernel: ring does not fit");
+    const size_t smem = 128 + stages * stage_bytes;
+    unsigned threads = (unsigned)std::min(256, ((rows * nvx + 31) / 32) * 32);
+    int per_sm = 0;
+    for (int mode : {lbm::MODE_STEP, lbm::MODE_STEP_MACRO}) {
+        const void *k = staged_ptr(h->prec, mode);
+        LBM_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    }
+    LBM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, staged_ptr(h->prec, lbm::MODE_STEP),
+                                                           (int)threads, smem));
+    if (per_sm < 1) return fail(LBM_EINVAL, "staged kernel: no resident block");
+    h->rows = rows;
+    h->gpp = (dim - 2 + rows - 1) / rows;
+    h->ngroups = (unsigned)h->gpp * (unsigned)(dim - 2);
+    h->stages = stages;
+    h->sblock = threads;
+    h->ssmem = smem;
+    h->sgrid = (unsigned)std::min<size_t>(h->ngroups, (size_t)per_sm * nsm);
+    return LBM_OK;
 }
 
 cudaError_t launch_pull(const lbm_t *h, int mode, const lbm::StepArgs &a)
 {
+    if (h->kernel == LBM_KERNEL_STAGED && mode != lbm::MODE_REDUCE) {
+        switch (h->prec) {
+        case LBM_FP32: return lbm::launch_staged_f32(mode, a, h->sgrid, h->sblock, h->ssmem, h->stream);
+        case LBM_FP64: return lbm::launch_staged_f64(mode, a, h->sgrid, h->sblock, h->ssmem, h->stream);
+        case LBM_FP16: return lbm::launch_staged_f16(mode, a, h->sgrid, h->sblock, h->ssmem, h->stream);
+        default: return lbm::launch_staged_bf16(mode, a, h->sgrid, h->sblock, h->ssmem, h->stream);
+        }
+    }
     switch (h->prec) {
     case LBM_FP32: return lbm::launch_pull_f32(mode, a, h->grid, h->block, h->stream);
     case LBM_FP64: return lbm::launch_pull_f64(mode, a, h->grid, h->block, h->stream);
@@ -262,6 +328,9 @@ int lbm_init(lbm_t **out, const lbm_config *c)
     if (!std::isfinite(c->velocity)) return fail(LBM_EINVAL, "lbm_init: velocity must be finite");
     if (c->noise_sigma < 0.0 || !std::isfinite(c->noise_sigma))
         return fail(LBM_EINVAL, "lbm_init: noise_sigma must be finite and >= 0");
+    if (c->kernel < LBM_KERNEL_AUTO || c->kernel > LBM_KERNEL_STAGED)
+        return fail(LBM_EINVAL, "lbm_init: unknown kernel variant %d", c->kernel);
+    if (c->stages < 0 || c->stages > 16) return fail(LBM_EINVAL, "lbm_init: stages %d out of range", c->stages);
     if (c->block_threads < 0 || c->block_threads > 1024)
         return fail(LBM_EINVAL, "lbm_init: block_threads %d out of range", c->block_threads);
     if (c->lid_profile) {
@@ -358,6 +427,16 @@ int lbm_init(lbm_t **out, const lbm_config *c)
         LBM_CUDA(cudaEventRecord(h->ev_last, h->stream));
         // the copy source (lidh) must outlive the copy
         LBM_CUDA(cudaStreamSynchronize(h->stream));
+
+        // iteration kernel: 16-bit storage defaults to the staged variant
+        int want = c->kernel;
+        if (want == LBM_KERNEL_AUTO) want = (prec == LBM_FP16 || prec == LBM_BF16) ? LBM_KERNEL_STAGED : LBM_KERNEL_DIRECT;
+        h->kernel = LBM_KERNEL_DIRECT;
+        if (want == LBM_KERNEL_STAGED) {
+            const int r = setup_staged(h, c->stages);
+            if (r == LBM_OK) h->kernel = LBM_KERNEL_STAGED;
+            else if (c->kernel == LBM_KERNEL_STAGED) return r;  // asked for explicitly
+        }
         return LBM_OK;
     };
     rc = setup();

@@ -294,6 +294,11 @@ struct StepArgs {
     size_t n;            // dim^3
     double inv_tau;      // 1/tau in the compute precision (rounded by the host)
     float omega_f;       // 1/tau as float, deviation kernels
+    // staged variant
+    int rows;            // rows per group
+    int gpp;             // groups per z-plane = ceil((dim-2) / rows)
+    unsigned ngroups;    // gpp * (dim-2)
+    int stages;          // ring depth
 };
 
 // Initial-state kernel arguments.

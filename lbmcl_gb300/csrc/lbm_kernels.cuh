@@ -267,12 +267,68 @@ __device__ __forceinline__ void block_reduce_write(double m, double e, double *p
 // ---------------------------------------------------------------------------
 // The fused pull-stream + collide iteration.
 // ---------------------------------------------------------------------------
+// Update the V sites x0..x0+V-1 of row (y, z) in place: fs holds their pulled
+// populations on entry and their post-collision populations on exit.  Stores
+// rho / u (MODE_STEP_MACRO) or accumulates the reduction sums (MODE_REDUCE).
+template <class S, int MODE, int V>
+__device__ __forceinline__ void update_vector(S (&fs)[Q][V], typename MapWord<V>::type mw, const StepArgs &a,
+                                              int y, int z, int x0, size_t site0, double &red_m, double &red_e)
+{
+    using C = typename Compute<S>::type;
+    constexpr bool DEV = is_dev16<S>();
+    const int dim = a.dim;
+    const bool lid_row = (z == dim - 2);
+    const C *lid = static_cast<const C *>(a.lid);
+    const Weights<C> W = make_weights<C>();
+    const C inv_tau = (C)a.inv_tau;
+    bool bad = false;
+
+#pragma unroll
+    for (int k = 0; k < V; ++k) {
+        const uint8_t b = (uint8_t)(mw >> (8 * k));
+        const C lidv = lid_row ? lid[(size_t)y * dim + x0 + k] : (C)0;
+        SiteOut o;
+        if constexpr (DEV) {
+            float D[Q];
+#pragma unroll
+            for (int i = 0; i < Q; ++i) D[i] = Dev16<S>::to_f(fs[i][k]);
+            site_dev<MODE != MODE_REDUCE>(D, b, (float)lidv, a.omega_f, Dev16<S>::scale, Dev16<S>::inv_scale, o);
+#pragma unroll
+            for (int i = 0; i < Q; ++i) fs[i][k] = Dev16<S>::from_f(D[i]);
+        } else {
+            C f[Q];
+#pragma unroll
+            for (int i = 0; i < Q; ++i) f[i] = fs[i][k];
+            site_exact<C, MODE != MODE_REDUCE>(f, b, lidv, inv_tau, W, o);
+#pragma unroll
+            for (int i = 0; i < Q; ++i) fs[i][k] = f[i];
+        }
+        bad |= o.bad;
+        if (MODE == MODE_STEP_MACRO && o.macro) {
+            C *rho = static_cast<C *>(a.rho);
+            C *u = static_cast<C *>(a.u);
+            const size_t id = site0 + k;
+            rho[id] = (C)o.r;
+            u[id] = (C)o.ux;
+            u[a.n + id] = (C)o.uy;
+            u[2 * a.n + id] = (C)o.uz;
+        }
+        if (MODE == MODE_REDUCE && o.macro) {
+            red_m += o.r;
+            red_e += 0.5 * o.r * (o.ux * o.ux + o.uy * o.uy + o.uz * o.uz);
+        }
+    }
+    if (bad) atomicOr(a.status, 1);
+}
+
+// ---------------------------------------------------------------------------
+// Direct variant: every thread loads its V sites' populations with 16-byte
+// vector loads straight from HBM.
+// ---------------------------------------------------------------------------
 template <class S, int MODE>
 __global__ void __launch_bounds__(256) pull_kernel(StepArgs a)
 {
     constexpr int V = 16 / (int)sizeof(S);
-    using C = typename Compute<S>::type;
-    constexpr bool DEV = is_dev16<S>();
     const unsigned g = blockIdx.x * blockDim.x + threadIdx.x;
     double red_m = 0.0, red_e = 0.0;
 
@@ -286,54 +342,12 @@ __global__ void __launch_bounds__(256) pull_kernel(StepArgs a)
         const size_t rowoff = (size_t)z * dim * dim + (size_t)y * dim;
         const size_t site0 = rowoff + (size_t)x0;
 
-        typename MapWord<V>::type mw =
+        const typename MapWord<V>::type mw =
             __ldg(reinterpret_cast<const typename MapWord<V>::type *>(a.map + site0));
         const S *__restrict__ fin = static_cast<const S *>(a.fin);
         S fs[Q][V];
         gather_all<S, V, 0>(fin, a.n, rowoff, dim, x0, fs);
-
-        const bool lid_row = (z == dim - 2);
-        const C *lid = static_cast<const C *>(a.lid);
-        const Weights<C> W = make_weights<C>();
-        const C inv_tau = (C)a.inv_tau;
-        bool bad = false;
-
-#pragma unroll
-        for (int k = 0; k < V; ++k) {
-            const uint8_t b = (uint8_t)(mw >> (8 * k));
-            const C lidv = lid_row ? lid[(size_t)y * dim + x0 + k] : (C)0;
-            SiteOut o;
-            if constexpr (DEV) {
-                float D[Q];
-#pragma unroll
-                for (int i = 0; i < Q; ++i) D[i] = Dev16<S>::to_f(fs[i][k]);
-                site_dev<MODE != MODE_REDUCE>(D, b, (float)lidv, a.omega_f, Dev16<S>::scale, Dev16<S>::inv_scale, o);
-#pragma unroll
-                for (int i = 0; i < Q; ++i) fs[i][k] = Dev16<S>::from_f(D[i]);
-            } else {
-                C f[Q];
-#pragma unroll
-                for (int i = 0; i < Q; ++i) f[i] = fs[i][k];
-                site_exact<C, MODE != MODE_REDUCE>(f, b, lidv, inv_tau, W, o);
-#pragma unroll
-                for (int i = 0; i < Q; ++i) fs[i][k] = f[i];
-            }
-            bad |= o.bad;
-            if (MODE == MODE_STEP_MACRO && o.macro) {
-                C *rho = static_cast<C *>(a.rho);
-                C *u = static_cast<C *>(a.u);
-                const size_t id = site0 + k;
-                rho[id] = (C)o.r;
-                u[id] = (C)o.ux;
-                u[a.n + id] = (C)o.uy;
-                u[2 * a.n + id] = (C)o.uz;
-            }
-            if (MODE == MODE_REDUCE && o.macro) {
-                red_m += o.r;
-                red_e += 0.5 * o.r * (o.ux * o.ux + o.uy * o.uy + o.uz * o.uz);
-            }
-        }
-        if (bad) atomicOr(a.status, 1);
+        update_vector<S, MODE, V>(fs, mw, a, y, z, x0, site0, red_m, red_e);
 
         if (MODE != MODE_REDUCE) {
             S *__restrict__ fout = static_cast<S *>(a.fout);
@@ -342,6 +356,217 @@ __global__ void __launch_bounds__(256) pull_kernel(StepArgs a)
         }
     }
     if (MODE == MODE_REDUCE) block_reduce_write(red_m, red_e, a.partials);
+}
+
+// ---------------------------------------------------------------------------
+// Staged variant.  Persistent CTAs walk "row groups" (R consecutive interior
+// rows of one z-plane).  For each group one thread issues 19 cp.async.bulk
+// copies -- the R source rows of every population, which are contiguous in
+// the SoA layout -- into one stage of a shared-memory ring, completing on
+// that stage's mbarrier.  The ring keeps `stages` groups in flight while the
+// CTA's threads update the current group from shared memory (the +-x shifted
+// values are neighbouring shared-memory elements) and store the results with
+// vector stores.  Every mbarrier wait is bounded: on expiry the kernel sets
+// bit 1 of the status word, stops issuing copies, drains what it issued
+// (again bounded) and returns.
+// ---------------------------------------------------------------------------
+constexpr uint32_t kWaitLimit = 1u << 22;
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, uint32_t limit)
+{
+    for (uint32_t k = 0; k < limit; ++k)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+// Pull one population for V sites from a shared-memory row (values at x - EX).
+template <class S, int V, int EX>
+__device__ __forceinline__ void gather_smem(const S *row, int x0, int dim, S (&out)[V])
+{
+    static_assert((V * sizeof(S)) % 8 == 0, "8-byte multiples");
+    S v[V];
+    if constexpr (V * sizeof(S) == 8) {
+        const uint2 r = *reinterpret_cast<const uint2 *>(row + x0);
+        memcpy(v, &r, 8);
+    } else {
+#pragma unroll
+        for (int c = 0; c < (int)(V * sizeof(S) / 16); ++c) {
+            const uint4 r = *reinterpret_cast<const uint4 *>(reinterpret_cast<const char *>(row + x0) + 16 * c);
+            memcpy(reinterpret_cast<char *>(v) + 16 * c, &r, 16);
+        }
+    }
+    if constexpr (EX == 0) {
+#pragma unroll
+        for (int k = 0; k < V; ++k) out[k] = v[k];
+    } else if constexpr (EX == 1) {
+        out[0] = (x0 > 0) ? row[x0 - 1] : zero_elem<S>();
+#pragma unroll
+        for (int k = 1; k < V; ++k) out[k] = v[k - 1];
+    } else {
+#pragma unroll
+        for (int k = 0; k < V - 1; ++k) out[k] = v[k + 1];
+        out[V - 1] = (x0 + V < dim) ? row[x0 + V] : zero_elem<S>();
+    }
+}
+
+template <class S, int V, int I>
+__device__ __forceinline__ void gather_all_smem(const S *stage, int rowlen, int r, int dim, int x0, S (&fs)[Q][V])
+{
+    gather_smem<S, V, ex_of(I)>(stage + (size_t)I * rowlen + (size_t)r * dim, x0, dim, fs[I]);
+    if constexpr (I + 1 < Q) gather_all_smem<S, V, I + 1>(stage, rowlen, r, dim, x0, fs);
+}
+
+template <class S, int V>
+__device__ __forceinline__ void store_global(S *p, const S (&in)[V])
+{
+    if constexpr (V * sizeof(S) == 8) {
+        uint2 r;
+        memcpy(&r, in, 8);
+        *reinterpret_cast<uint2 *>(p) = r;
+    } else {
+#pragma unroll
+        for (int c = 0; c < (int)(V * sizeof(S) / 16); ++c) {
+            uint4 r;
+            memcpy(&r, reinterpret_cast<const char *>(in) + 16 * c, 16);
+            *reinterpret_cast<uint4 *>(reinterpret_cast<char *>(p) + 16 * c) = r;
+        }
+    }
+}
+
+// group g -> plane z, first row y0, rows in this group
+__device__ __forceinline__ void decode_group(const StepArgs &a, unsigned g, int &z, int &y0, int &reff)
+{
+    z = 1 + (int)(g / (unsigned)a.gpp);
+    y0 = 1 + (int)(g % (unsigned)a.gpp) * a.rows;
+    reff = min(a.rows, a.dim - 1 - y0);
+}
+
+template <class S>
+__device__ __forceinline__ void issue_group(const StepArgs &a, S *stage, uint64_t *bar, unsigned g)
+{
+    int z, y0, reff;
+    decode_group(a, g, z, y0, reff);
+    const int dim = a.dim;
+    const uint32_t bytes = (uint32_t)reff * (uint32_t)dim * (uint32_t)sizeof(S);
+    const size_t rowlen = (size_t)a.rows * dim;
+    mbar_expect_tx(bar, (uint32_t)Q * bytes);
+    const S *fin = static_cast<const S *>(a.fin);
+#pragma unroll
+    for (int i = 0; i < Q; ++i) {
+        const S *src = fin + (size_t)i * a.n + (size_t)(z - ez_of(i)) * dim * dim + (size_t)(y0 - ey_of(i)) * dim;
+        bulk_copy_g2s(stage + (size_t)i * rowlen, src, bytes, bar);
+    }
+}
+
+template <class S, int MODE>
+__global__ void __launch_bounds__(256) pull_staged_kernel(StepArgs a)
+{
+    constexpr int V = 4;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem_raw);
+    S *ring = reinterpret_cast<S *>(smem_raw + 128);
+    const int dim = a.dim;
+    const int ns = a.stages;
+    const int rowlen = a.rows * dim;
+    const size_t stage_elems = (size_t)Q * rowlen;
+    const unsigned G = a.ngroups;
+    const int nvx = dim / V;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < ns; ++s) mbar_init(&bars[s], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    unsigned issued = 0;  // groups issued by thread 0 (only thread 0 tracks it)
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < ns; ++s) {
+            const unsigned g = blockIdx.x + (unsigned)s * gridDim.x;
+            if (g < G) {
+                issue_group<S>(a, ring + (size_t)s * stage_elems, &bars[s], g);
+                ++issued;
+            }
+        }
+    }
+
+    bool err = false;
+    unsigned k = 0, fail_k = 0xffffffffu;
+    double red_m = 0.0, red_e = 0.0;
+    S *__restrict__ fout = static_cast<S *>(a.fout);
+    for (;; ++k) {
+        const unsigned g = blockIdx.x + k * gridDim.x;
+        if (g >= G) break;
+        const int s = (int)(k % (unsigned)ns);
+        const uint32_t parity = (k / (unsigned)ns) & 1u;
+        if (!err) {
+            err = !mbar_wait_bounded(&bars[s], parity, kWaitLimit);
+            if (err) fail_k = k;
+        }
+        if (!err) {
+            int z, y0, reff;
+            decode_group(a, g, z, y0, reff);
+            const S *stage = ring + (size_t)s * stage_elems;
+            for (int v = threadIdx.x; v < reff * nvx; v += blockDim.x) {
+                const int r = v / nvx;
+                const int x0 = (v - r * nvx) * V;
+                const int y = y0 + r;
+                const size_t site0 = (size_t)z * dim * dim + (size_t)y * dim + x0;
+                const typename MapWord<V>::type mw =
+                    __ldg(reinterpret_cast<const typename MapWord<V>::type *>(a.map + site0));
+                S fs[Q][V];
+                gather_all_smem<S, V, 0>(stage, rowlen, r, dim, x0, fs);
+                update_vector<S, MODE, V>(fs, mw, a, y, z, x0, site0, red_m, red_e);
+#pragma unroll
+                for (int i = 0; i < Q; ++i) store_global<S, V>(fout + (size_t)i * a.n + site0, fs[i]);
+            }
+        }
+        __syncthreads();  // stage s fully read before it is refilled
+        if (threadIdx.x == 0 && !err) {
+            const unsigned gn = g + (unsigned)ns * gridDim.x;
+            if (gn < G) {
+                issue_group<S>(a, ring + (size_t)s * stage_elems, &bars[s], gn);
+                ++issued;
+            }
+        }
+    }
+    if (err) {
+        atomicOr(a.status, 2);
+        // drain the copies this CTA issued and never consumed (bounded)
+        if (threadIdx.x == 0) {
+            for (unsigned j = fail_k; j < issued; ++j)
+                mbar_wait_bounded(&bars[j % (unsigned)ns], (j / (unsigned)ns) & 1u, kWaitLimit);
+        }
+    }
 }
 
 // ---------------------------------------------------------------------------

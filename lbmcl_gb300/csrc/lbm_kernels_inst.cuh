@@ -32,6 +32,27 @@ const void *LBM_CAT(pull_kernel_ptr_, LBM_SFX)(int mode)
     }
 }
 
+cudaError_t LBM_CAT(launch_staged_, LBM_SFX)(int mode, const StepArgs &a, unsigned grid, unsigned block,
+                                             size_t smem, cudaStream_t s)
+{
+    if (grid == 0) return cudaSuccess;
+    switch (mode) {
+    case MODE_STEP: pull_staged_kernel<LBM_S, MODE_STEP><<<grid, block, smem, s>>>(a); break;
+    case MODE_STEP_MACRO: pull_staged_kernel<LBM_S, MODE_STEP_MACRO><<<grid, block, smem, s>>>(a); break;
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+const void *LBM_CAT(staged_kernel_ptr_, LBM_SFX)(int mode)
+{
+    switch (mode) {
+    case MODE_STEP: return (const void *)pull_staged_kernel<LBM_S, MODE_STEP>;
+    case MODE_STEP_MACRO: return (const void *)pull_staged_kernel<LBM_S, MODE_STEP_MACRO>;
+    default: return nullptr;
+    }
+}
+
 cudaError_t LBM_CAT(launch_init_, LBM_SFX)(const InitArgs &a, cudaStream_t s)
 {
     const unsigned block = 256;

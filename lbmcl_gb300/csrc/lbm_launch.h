@@ -18,7 +18,10 @@ struct DumpArgs;
     cudaError_t launch_init_##SFX(const InitArgs &a, cudaStream_t s);                               \
     cudaError_t launch_dump_##SFX(const DumpArgs &a, cudaStream_t s);                               \
     cudaError_t launch_load_##SFX(const DumpArgs &a, cudaStream_t s);                               \
-    const void *pull_kernel_ptr_##SFX(int mode);
+    const void *pull_kernel_ptr_##SFX(int mode);                                                    \
+    cudaError_t launch_staged_##SFX(int mode, const StepArgs &a, unsigned grid, unsigned block,      \
+                                    size_t smem, cudaStream_t s);                                    \
+    const void *staged_kernel_ptr_##SFX(int mode);
 
 LBM_DECLARE_LAUNCHERS(f32)
 LBM_DECLARE_LAUNCHERS(f64)

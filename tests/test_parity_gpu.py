@@ -35,13 +35,15 @@ def test_map_bit_exact(capi, oracle, dim):
         np.testing.assert_array_equal(L.cell_map(), oracle.cell_types(dim))
 
 
+@pytest.mark.parametrize("kernel", ["direct", "staged"])
 @pytest.mark.parametrize("prec", ["f32", "f64"])
 @pytest.mark.parametrize("dim,stride", [(8, 8), (32, 8), (16, 1), (16, 4096), (4, 4), (12, 16)])
-def test_f_after_each_step(capi, oracle, prec, dim, stride):
+def test_f_after_each_step(capi, oracle, prec, dim, stride, kernel):
     """Config 1 shape (32^3, stride 8, 10 steps) and layout / size variations:
-    the full post-stream buffer, wall slots included, after every iteration."""
+    the full post-stream buffer, wall slots included, after every iteration,
+    for both iteration-kernel variants."""
     o = oracle.OracleLattice(dim, 0.0089, 0.05, prec, stride)
-    with capi.Lattice(dim, 0.0089, 0.05, precision=GPU_PREC[prec], stride=stride) as L:
+    with capi.Lattice(dim, 0.0089, 0.05, precision=GPU_PREC[prec], stride=stride, kernel=kernel) as L:
         assert_f_close(L.f(), o.state, TOL[prec], "initial")
         for it in range(1, 11):
             o.step(1, every=1)
@@ -53,8 +55,9 @@ def test_f_after_each_step(capi, oracle, prec, dim, stride):
             np.testing.assert_array_equal(bits(L.u()), bits(o.u))
 
 
+@pytest.mark.parametrize("kernel", ["direct", "staged"])
 @pytest.mark.parametrize("prec", ["f32", "f64"])
-def test_lid_profile_noise_and_macro_every(capi, oracle, prec):
+def test_lid_profile_noise_and_macro_every(capi, oracle, prec, kernel):
     """Per-column lid, seeded noise on FLUID populations, macros every 3rd
     iteration; 60 iterations at 24^3 with block-size and stride changes."""
     rng = np.random.default_rng(11)
@@ -62,7 +65,7 @@ def test_lid_profile_noise_and_macro_every(capi, oracle, prec):
     lid = 0.05 + 0.01 * rng.standard_normal(dim * dim)
     o = oracle.OracleLattice(dim, 0.01, 0.05, prec, 64, lid=lid, seed=1234, noise_sigma=1e-4)
     with capi.Lattice(dim, 0.01, 0.05, precision=GPU_PREC[prec], stride=64, lid=lid, seed=1234,
-                      noise_sigma=1e-4, block_threads=96) as L:
+                      noise_sigma=1e-4, block_threads=96, kernel=kernel) as L:
         assert np.array_equal(bits(L.f()), bits(o.state)), "initial state (noise) differs"
         for chunk in (1, 2, 7, 20, 30):
             o.step(chunk, every=3)
@@ -96,10 +99,12 @@ def test_golden_sailfish_8_and_32(capi):
             assert c["mae_rho"] < 5e-6 and c["mae_v"] < 2e-6, (it, c)
 
 
+@pytest.mark.parametrize("kernel", ["direct", "staged"])
 @pytest.mark.parametrize("prec", ["f32", "f64"])
-def test_64cube_200_steps(capi, oracle, prec):
+def test_64cube_200_steps(capi, oracle, prec, kernel):
     o = oracle.OracleLattice(64, 0.0089, 0.05, prec, 64, seed=7, noise_sigma=1e-4)
-    with capi.Lattice(64, 0.0089, 0.05, precision=GPU_PREC[prec], stride=64, seed=7, noise_sigma=1e-4) as L:
+    with capi.Lattice(64, 0.0089, 0.05, precision=GPU_PREC[prec], stride=64, seed=7, noise_sigma=1e-4,
+                      kernel=kernel) as L:
         o.step(200, every=100)
         L.step(200, every=100)
         g = L.f()
@@ -208,3 +213,21 @@ def test_deterministic_repeat(capi):
             L.step(40)
             outs.append(L.raw())
     np.testing.assert_array_equal(outs[0], outs[1])
+
+
+@pytest.mark.parametrize("prec", ["fp32", "fp64", "fp16", "bf16"])
+@pytest.mark.parametrize("dim,stages", [(8, 2), (24, 3), (64, 0), (136, 5), (256, 0)])
+def test_staged_equals_direct(capi, prec, dim, stages):
+    """The two iteration kernels move data differently but run the same site
+    update: their raw population buffers agree bit for bit (incl. macros)."""
+    outs = []
+    for kernel in ("direct", "staged"):
+        with capi.Lattice(dim, 0.005, 0.08, precision=prec, seed=21, noise_sigma=1e-4, kernel=kernel,
+                          stages=stages) as L:
+            L.step(7)
+            L.step(6, every=6)
+            L.sync()
+            outs.append((L.raw(), L.rho(), L.u()))
+    np.testing.assert_array_equal(outs[0][0], outs[1][0])
+    np.testing.assert_array_equal(bits(outs[0][1]), bits(outs[1][1]))
+    np.testing.assert_array_equal(bits(outs[0][2]), bits(outs[1][2]))
