@@ -96,8 +96,9 @@ typedef struct lbm_config {
 typedef enum lbm_kernel {
     LBM_KERNEL_AUTO = 0,
     LBM_KERNEL_DIRECT = 1,   /* per-thread 16-byte vector loads straight from HBM        */
-    LBM_KERNEL_STAGED = 2    /* persistent CTAs; whole source rows staged in shared
+    LBM_KERNEL_STAGED = 2,   /* persistent CTAs; whole source rows staged in shared
                                 memory by cp.async.bulk (TMA) through an mbarrier ring   */
+    LBM_KERNEL_NARROW = 3    /* as DIRECT with 8-byte vectors (fewer registers)          */
 } lbm_kernel;
 
 /* Fill *c with the reference CLI defaults (lbm_options.hpp:83-101):

@@ -119,6 +119,7 @@ struct lbm_handle {
     int kernel = LBM_KERNEL_DIRECT;
     int rows = 1, gpp = 0, stages = 0;
     unsigned ngroups = 0, sgrid = 0, sblock = 0;
+    unsigned ngrid = 0;     // narrow variant: grid over 8-byte vectors
     size_t ssmem = 0;
 };
 
@@ -258,6 +259,17 @@ cudaError_t launch_pull(const lbm_t *h, int mode, const lbm::StepArgs &a)
         default: return lbm::launch_staged_bf16(mode, a, h->sgrid, h->sblock, h->ssmem, h->stream);
         }
     }
+    if (h->kernel == LBM_KERNEL_NARROW && mode != lbm::MODE_REDUCE) {
+        // half-width vectors: twice as many threads, each owning V/2 sites
+        lbm::StepArgs n = a;
+        n.nvx = 2 * a.nvx;
+        n.nvec = 2 * a.nvec;
+        switch (h->prec) {
+        case LBM_FP32: return lbm::launch_narrow_f32(mode, n, h->ngrid, h->block, h->stream);
+        case LBM_FP16: return lbm::launch_narrow_f16(mode, n, h->ngrid, h->block, h->stream);
+        default: return lbm::launch_narrow_bf16(mode, n, h->ngrid, h->block, h->stream);
+        }
+    }
     switch (h->prec) {
     case LBM_FP32: return lbm::launch_pull_f32(mode, a, h->grid, h->block, h->stream);
     case LBM_FP64: return lbm::launch_pull_f64(mode, a, h->grid, h->block, h->stream);
@@ -328,7 +340,7 @@ int lbm_init(lbm_t **out, const lbm_config *c)
     if (!std::isfinite(c->velocity)) return fail(LBM_EINVAL, "lbm_init: velocity must be finite");
     if (c->noise_sigma < 0.0 || !std::isfinite(c->noise_sigma))
         return fail(LBM_EINVAL, "lbm_init: noise_sigma must be finite and >= 0");
-    if (c->kernel < LBM_KERNEL_AUTO || c->kernel > LBM_KERNEL_STAGED)
+    if (c->kernel < LBM_KERNEL_AUTO || c->kernel > LBM_KERNEL_NARROW)
         return fail(LBM_EINVAL, "lbm_init: unknown kernel variant %d", c->kernel);
     if (c->stages < 0 || c->stages > 16) return fail(LBM_EINVAL, "lbm_init: stages %d out of range", c->stages);
     if (c->block_threads < 0 || c->block_threads > 1024)
@@ -344,7 +356,7 @@ int lbm_init(lbm_t **out, const lbm_config *c)
     if (block < 32) block = 32;
     if (block > 256) block = 256;  // the pull kernel's launch bound
     const size_t grid = (nvec + block - 1) / block;
-    if (nvec >= ((size_t)1 << 32)) return fail(LBM_EINVAL, "lbm_init: lattice too large");
+    if (2 * nvec >= ((size_t)1 << 32)) return fail(LBM_EINVAL, "lbm_init: lattice too large");
 
     const size_t sb = storage_bytes(prec), mb = macro_bytes(prec);
     const size_t fbytes = (size_t)lbm::Q * n * sb;
@@ -432,6 +444,10 @@ int lbm_init(lbm_t **out, const lbm_config *c)
         int want = c->kernel;
         if (want == LBM_KERNEL_AUTO) want = (prec == LBM_FP16 || prec == LBM_BF16) ? LBM_KERNEL_STAGED : LBM_KERNEL_DIRECT;
         h->kernel = LBM_KERNEL_DIRECT;
+        if (want == LBM_KERNEL_NARROW && prec != LBM_FP64) {
+            h->kernel = LBM_KERNEL_NARROW;
+            h->ngrid = (unsigned)((2 * nvec + block - 1) / block);
+        }
         if (want == LBM_KERNEL_STAGED) {
             const int r = setup_staged(h, c->stages);
             if (r == LBM_OK) h->kernel = LBM_KERNEL_STAGED;

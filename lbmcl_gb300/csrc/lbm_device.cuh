@@ -233,18 +233,33 @@ __device__ __forceinline__ T init_eq_exact(int i, T lid, const Weights<T> &W)
 // 16-bit deviation storage: a population is held as D = s (f - w) in FP16
 // (s = 2^15) or BF16 (s = 1); all arithmetic is FP32 with FMAs.
 // ---------------------------------------------------------------------------
-template <class H> struct Dev16;
+template <class H> struct Dev16 {  // not a 16-bit type: unused placeholders
+    static constexpr float scale = 1.0f;
+    static constexpr float inv_scale = 1.0f;
+};
 template <> struct Dev16<__half> {
     static constexpr float scale = 32768.0f;
     static constexpr float inv_scale = 1.0f / 32768.0f;
     static __device__ __forceinline__ float to_f(__half h) { return __half2float(h); }
     static __device__ __forceinline__ __half from_f(float v) { return __float2half_rn(v); }
+    static __device__ __forceinline__ void from_f2(float a, float b, __half &ha, __half &hb)
+    {
+        const __half2 h = __floats2half2_rn(a, b);  // one packed conversion
+        ha = __low2half(h);
+        hb = __high2half(h);
+    }
 };
 template <> struct Dev16<__nv_bfloat16> {
     static constexpr float scale = 1.0f;
     static constexpr float inv_scale = 1.0f;
     static __device__ __forceinline__ float to_f(__nv_bfloat16 h) { return __bfloat162float(h); }
     static __device__ __forceinline__ __nv_bfloat16 from_f(float v) { return __float2bfloat16_rn(v); }
+    static __device__ __forceinline__ void from_f2(float a, float b, __nv_bfloat16 &ha, __nv_bfloat16 &hb)
+    {
+        const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+        ha = __low2bfloat16(h);
+        hb = __high2bfloat16(h);
+    }
 };
 
 __host__ __device__ constexpr float wf_of(int i)

@@ -32,16 +32,27 @@ template <class S> __host__ __device__ constexpr bool is_dev16() { return sizeof
 template <class S, int V>
 __device__ __forceinline__ void load_vec(const S *__restrict__ p, S (&out)[V])
 {
-    static_assert(V * sizeof(S) == 16, "16-byte vectors");
-    const uint4 r = __ldg(reinterpret_cast<const uint4 *>(p));
-    memcpy(out, &r, 16);
+    static_assert(V * sizeof(S) == 16 || V * sizeof(S) == 8, "8- or 16-byte vectors");
+    if constexpr (V * sizeof(S) == 16) {
+        const uint4 r = __ldg(reinterpret_cast<const uint4 *>(p));
+        memcpy(out, &r, 16);
+    } else {
+        const uint2 r = __ldg(reinterpret_cast<const uint2 *>(p));
+        memcpy(out, &r, 8);
+    }
 }
 template <class S, int V>
 __device__ __forceinline__ void store_vec(S *__restrict__ p, const S (&in)[V])
 {
-    uint4 r;
-    memcpy(&r, in, 16);
-    *reinterpret_cast<uint4 *>(p) = r;
+    if constexpr (V * sizeof(S) == 16) {
+        uint4 r;
+        memcpy(&r, in, 16);
+        *reinterpret_cast<uint4 *>(p) = r;
+    } else {
+        uint2 r;
+        memcpy(&r, in, 8);
+        *reinterpret_cast<uint2 *>(p) = r;
+    }
 }
 template <class S> __device__ __forceinline__ S load_one(const S *__restrict__ p)
 {
@@ -169,59 +180,124 @@ __device__ __forceinline__ void site_exact(T (&f)[Q], uint8_t b, T lidv, T inv_t
     }
 }
 
-// 16-bit deviation site update.  D holds s (f - w) as FP32.
+// ---------------------------------------------------------------------------
+// 16-bit deviation site update.  D holds s (f - w) as FP32.  Written for a
+// low instruction count (the 16-bit kernels move half the bytes per site, so
+// issue rate, not HBM, limits them otherwise): moments from opposite-pair sums
+// and differences, and the BGK update of each opposite pair (i, -i) with
+// e_i . u = +-a as
+//     D'_(+-) = (1 - w) D_(+-) + K_c (drho + rho (4.5 a^2 - 1.5 u^2)) +- 3 K_c rho a,
+// K_c = omega s w_c.  Every operation is an explicit IEEE intrinsic, so the
+// result does not depend on where the compiler inlines it.
+// ---------------------------------------------------------------------------
+struct DevK {
+    float keep;   // 1 - omega
+    float k[3];   // omega * s * w_c
+    float k3[3];  // 3 omega s w_c
+    float inv_s;
+};
+
+__device__ __forceinline__ DevK make_devk(float omega, float s, float inv_s)
+{
+    DevK K;
+    K.keep = __fsub_rn(1.0f, omega);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const float w = c == 0 ? (1.0f / 3.0f) : (c == 1 ? (1.0f / 18.0f) : (1.0f / 36.0f));
+        K.k[c] = __fmul_rn(__fmul_rn(omega, s), w);
+        K.k3[c] = __fmul_rn(3.0f, K.k[c]);
+    }
+    K.inv_s = inv_s;
+    return K;
+}
+
+__device__ __forceinline__ void relax_pair_dev(float &dp, float &dm, float a, int c, float rho, float drho, float c15,
+                                               const DevK &K)
+{
+    const float p = __fmaf_rn(__fmul_rn(4.5f, a), a, -c15);
+    const float X = __fmaf_rn(rho, p, drho);
+    const float lin = __fmul_rn(__fmul_rn(K.k3[c], rho), a);
+    dp = __fmaf_rn(K.keep, dp, __fmaf_rn(K.k[c], X, lin));
+    dm = __fmaf_rn(K.keep, dm, __fmaf_rn(K.k[c], X, -lin));
+}
+
+// FLUID site in deviation form.
 template <bool COLLIDE>
-__device__ __forceinline__ void site_dev(float (&D)[Q], uint8_t b, float lidv, float omega, float s, float inv_s,
-                                         SiteOut &o)
+__device__ __forceinline__ void fluid_dev(float (&D)[Q], const DevK &K, SiteOut &o)
+{
+    const float s13 = __fadd_rn(D[1], D[3]), d13 = __fsub_rn(D[1], D[3]);
+    const float s24 = __fadd_rn(D[2], D[4]), d24 = __fsub_rn(D[2], D[4]);
+    const float s56 = __fadd_rn(D[5], D[6]), d65 = __fsub_rn(D[6], D[5]);
+    const float s79 = __fadd_rn(D[7], D[9]), d79 = __fsub_rn(D[7], D[9]);         // e7 = (+1,+1, 0)
+    const float s810 = __fadd_rn(D[8], D[10]), d810 = __fsub_rn(D[8], D[10]);     // e8 = (-1,+1, 0)
+    const float s1117 = __fadd_rn(D[11], D[17]), d1117 = __fsub_rn(D[11], D[17]); // e11 = (+1, 0,-1)
+    const float s1218 = __fadd_rn(D[12], D[18]), d1218 = __fsub_rn(D[12], D[18]); // e12 = ( 0,+1,-1)
+    const float s1315 = __fadd_rn(D[13], D[15]), d1513 = __fsub_rn(D[15], D[13]); // e15 = (+1, 0,+1)
+    const float s1416 = __fadd_rn(D[14], D[16]), d1614 = __fsub_rn(D[16], D[14]); // e16 = ( 0,+1,+1)
+    const float sd = __fadd_rn(__fadd_rn(D[0], s1416),
+                               __fadd_rn(__fadd_rn(__fadd_rn(s13, s24), __fadd_rn(s56, s79)),
+                                         __fadd_rn(__fadd_rn(s810, s1117), __fadd_rn(s1218, s1315))));
+    const float jx = __fadd_rn(__fsub_rn(__fadd_rn(d13, d79), d810), __fadd_rn(d1117, d1513));
+    const float jy = __fadd_rn(__fadd_rn(__fadd_rn(d24, d79), d810), __fadd_rn(d1218, d1614));
+    const float jz = __fadd_rn(__fsub_rn(__fsub_rn(d65, d1117), d1218), __fadd_rn(d1513, d1614));
+    const float drho = __fmul_rn(sd, K.inv_s);
+    const float rho = __fadd_rn(1.0f, drho);
+    const float kk = __fmul_rn(K.inv_s, __fdividef(1.0f, rho));
+    const float ux = __fmul_rn(jx, kk), uy = __fmul_rn(jy, kk), uz = __fmul_rn(jz, kk);
+    o.macro = true;
+    o.bad = !(rho > 0.0f);
+    o.r = rho; o.ux = ux; o.uy = uy; o.uz = uz;
+    if (!COLLIDE) return;
+    const float c15 = __fmul_rn(1.5f, __fmaf_rn(ux, ux, __fmaf_rn(uy, uy, __fmul_rn(uz, uz))));
+    D[0] = __fmaf_rn(K.keep, D[0], __fmul_rn(K.k[0], __fmaf_rn(rho, -c15, drho)));
+    relax_pair_dev(D[1], D[3], ux, 1, rho, drho, c15, K);
+    relax_pair_dev(D[2], D[4], uy, 1, rho, drho, c15, K);
+    relax_pair_dev(D[6], D[5], uz, 1, rho, drho, c15, K);
+    relax_pair_dev(D[7], D[9], __fadd_rn(ux, uy), 2, rho, drho, c15, K);
+    relax_pair_dev(D[8], D[10], __fsub_rn(uy, ux), 2, rho, drho, c15, K);
+    relax_pair_dev(D[11], D[17], __fsub_rn(ux, uz), 2, rho, drho, c15, K);
+    relax_pair_dev(D[12], D[18], __fsub_rn(uy, uz), 2, rho, drho, c15, K);
+    relax_pair_dev(D[15], D[13], __fadd_rn(ux, uz), 2, rho, drho, c15, K);
+    relax_pair_dev(D[16], D[14], __fadd_rn(uy, uz), 2, rho, drho, c15, K);
+}
+
+// Any site in deviation form (walls, faces, corners, lid, fluid).
+template <bool COLLIDE>
+__device__ __forceinline__ void site_dev(float (&D)[Q], uint8_t b, float lidv, const DevK &K, float s, SiteOut &o)
 {
     o.macro = false;
     o.bad = false;
-    if (b & M_WALL) return;
-    if (b != 0) {
-#pragma unroll
-        for (int i = 0; i < Q; ++i)
-            if (wall_sourced(i, b)) {
-                if (b & M_FRONT) {
-                    const float eu = ex_of(i) > 0 ? lidv : (ex_of(i) < 0 ? -lidv : 0.0f);
-                    D[i] = deq_scaled(i, 0.0f, 1.0f, eu, 1.5f * lidv * lidv, s);
-                } else {
-                    D[i] = 0.0f;
-                }
-            }
+    if (b == 0) {
+        fluid_dev<COLLIDE>(D, K, o);
+        return;
     }
-    if (b == 0 || b == M_FRONT) {
-        if (b == M_FRONT) { D[5] = D[6]; D[11] = D[17]; D[12] = D[18]; D[13] = D[15]; D[14] = D[16]; }
+    if (b & M_WALL) return;
+#pragma unroll
+    for (int i = 0; i < Q; ++i)
+        if (wall_sourced(i, b)) {
+            if (b & M_FRONT) {
+                const float eu = ex_of(i) > 0 ? lidv : (ex_of(i) < 0 ? -lidv : 0.0f);
+                D[i] = deq_scaled(i, 0.0f, 1.0f, eu, 1.5f * lidv * lidv, s);
+            } else {
+                D[i] = 0.0f;
+            }
+        }
+    if (b == M_FRONT) {
+        // moving lid: wall-sourced -z populations take their +z opposites, then
+        // the site is set to the equilibrium at its density and the lid velocity
+        D[5] = D[6]; D[11] = D[17]; D[12] = D[18]; D[13] = D[15]; D[14] = D[16];
         float sd = 0.0f;
 #pragma unroll
         for (int i = 0; i < Q; ++i) sd += D[i];
-        const float drho = sd * inv_s;
+        const float drho = sd * K.inv_s;
         const float rho = 1.0f + drho;
-        float ux, uy, uz;
-        if (b == 0) {
-            const float jx = ((D[1] + D[7]) + (D[10] + D[11]) + D[15]) - ((D[3] + D[8]) + (D[9] + D[13]) + D[17]);
-            const float jy = ((D[2] + D[7]) + (D[8] + D[12]) + D[16]) - ((D[4] + D[9]) + (D[10] + D[14]) + D[18]);
-            const float jz = ((D[6] + D[15]) + (D[16] + D[17]) + D[18]) - ((D[5] + D[11]) + (D[12] + D[13]) + D[14]);
-            const float k = inv_s * __frcp_rn(rho);
-            ux = jx * k; uy = jy * k; uz = jz * k;
-        } else {
-            ux = lidv; uy = 0.0f; uz = 0.0f;
-        }
         o.macro = true;
         o.bad = !(rho > 0.0f);
-        o.r = rho; o.ux = ux; o.uy = uy; o.uz = uz;
+        o.r = rho; o.ux = lidv; o.uy = 0.0f; o.uz = 0.0f;
         if (COLLIDE) {
-            const float c15 = 1.5f * fmaf(ux, ux, fmaf(uy, uy, uz * uz));
-            if (b == 0) {
-                const float keep = 1.0f - omega;
+            const float c15 = 1.5f * lidv * lidv;
 #pragma unroll
-                for (int i = 0; i < Q; ++i) {
-                    const float deq = deq_scaled(i, drho, rho, proj_fast(i, ux, uy, uz), c15, s);
-                    D[i] = fmaf(keep, D[i], omega * deq);
-                }
-            } else {
-#pragma unroll
-                for (int i = 0; i < Q; ++i) D[i] = deq_scaled(i, drho, rho, proj_fast(i, ux, uy, uz), c15, s);
-            }
+            for (int i = 0; i < Q; ++i) D[i] = deq_scaled(i, drho, rho, proj_fast(i, lidv, 0.0f, 0.0f), c15, s);
         }
         return;
     }
@@ -267,6 +343,23 @@ __device__ __forceinline__ void block_reduce_write(double m, double e, double *p
 // ---------------------------------------------------------------------------
 // The fused pull-stream + collide iteration.
 // ---------------------------------------------------------------------------
+template <class C>
+__device__ __forceinline__ void store_macro(const StepArgs &a, size_t id, const SiteOut &o)
+{
+    C *rho = static_cast<C *>(a.rho);
+    C *u = static_cast<C *>(a.u);
+    rho[id] = (C)o.r;
+    u[id] = (C)o.ux;
+    u[a.n + id] = (C)o.uy;
+    u[2 * a.n + id] = (C)o.uz;
+}
+
+__device__ __forceinline__ void accumulate(const SiteOut &o, double &m, double &e)
+{
+    m += o.r;
+    e += 0.5 * o.r * (o.ux * o.ux + o.uy * o.uy + o.uz * o.uz);
+}
+
 // Update the V sites x0..x0+V-1 of row (y, z) in place: fs holds their pulled
 // populations on entry and their post-collision populations on exit.  Stores
 // rho / u (MODE_STEP_MACRO) or accumulates the reduction sums (MODE_REDUCE).
@@ -283,6 +376,41 @@ __device__ __forceinline__ void update_vector(S (&fs)[Q][V], typename MapWord<V>
     const C inv_tau = (C)a.inv_tau;
     bool bad = false;
 
+    const DevK K = make_devk(a.omega_f, Dev16<S>::scale, Dev16<S>::inv_scale);
+    if constexpr (DEV) {
+        if (mw == 0) {
+            // all V sites FLUID (the bulk of the lattice): no per-site branches,
+            // two sites per step so the output converts as packed pairs
+#pragma unroll
+            for (int k = 0; k < V; k += 2) {
+                float D0[Q], D1[Q];
+#pragma unroll
+                for (int i = 0; i < Q; ++i) {
+                    D0[i] = Dev16<S>::to_f(fs[i][k]);
+                    D1[i] = Dev16<S>::to_f(fs[i][k + 1]);
+                }
+                SiteOut o0, o1;
+                fluid_dev<MODE != MODE_REDUCE>(D0, K, o0);
+                fluid_dev<MODE != MODE_REDUCE>(D1, K, o1);
+                bad |= o0.bad | o1.bad;
+                if (MODE != MODE_REDUCE) {
+#pragma unroll
+                    for (int i = 0; i < Q; ++i) Dev16<S>::from_f2(D0[i], D1[i], fs[i][k], fs[i][k + 1]);
+                }
+                if (MODE == MODE_STEP_MACRO) {
+                    store_macro<C>(a, site0 + k, o0);
+                    store_macro<C>(a, site0 + k + 1, o1);
+                }
+                if (MODE == MODE_REDUCE) {
+                    accumulate(o0, red_m, red_e);
+                    accumulate(o1, red_m, red_e);
+                }
+            }
+            if (bad) atomicOr(a.status, 1);
+            return;
+        }
+    }
+
 #pragma unroll
     for (int k = 0; k < V; ++k) {
         const uint8_t b = (uint8_t)(mw >> (8 * k));
@@ -292,7 +420,7 @@ __device__ __forceinline__ void update_vector(S (&fs)[Q][V], typename MapWord<V>
             float D[Q];
 #pragma unroll
             for (int i = 0; i < Q; ++i) D[i] = Dev16<S>::to_f(fs[i][k]);
-            site_dev<MODE != MODE_REDUCE>(D, b, (float)lidv, a.omega_f, Dev16<S>::scale, Dev16<S>::inv_scale, o);
+            site_dev<MODE != MODE_REDUCE>(D, b, (float)lidv, K, Dev16<S>::scale, o);
 #pragma unroll
             for (int i = 0; i < Q; ++i) fs[i][k] = Dev16<S>::from_f(D[i]);
         } else {
@@ -304,31 +432,20 @@ __device__ __forceinline__ void update_vector(S (&fs)[Q][V], typename MapWord<V>
             for (int i = 0; i < Q; ++i) fs[i][k] = f[i];
         }
         bad |= o.bad;
-        if (MODE == MODE_STEP_MACRO && o.macro) {
-            C *rho = static_cast<C *>(a.rho);
-            C *u = static_cast<C *>(a.u);
-            const size_t id = site0 + k;
-            rho[id] = (C)o.r;
-            u[id] = (C)o.ux;
-            u[a.n + id] = (C)o.uy;
-            u[2 * a.n + id] = (C)o.uz;
-        }
-        if (MODE == MODE_REDUCE && o.macro) {
-            red_m += o.r;
-            red_e += 0.5 * o.r * (o.ux * o.ux + o.uy * o.uy + o.uz * o.uz);
-        }
+        if (MODE == MODE_STEP_MACRO && o.macro) store_macro<C>(a, site0 + k, o);
+        if (MODE == MODE_REDUCE && o.macro) accumulate(o, red_m, red_e);
     }
     if (bad) atomicOr(a.status, 1);
 }
 
 // ---------------------------------------------------------------------------
-// Direct variant: every thread loads its V sites' populations with 16-byte
-// vector loads straight from HBM.
+// Direct variant: every thread loads its V sites' populations with VB-byte
+// vector loads straight from HBM (V = VB / sizeof(S)).
 // ---------------------------------------------------------------------------
-template <class S, int MODE>
+template <class S, int MODE, int VB = 16>
 __global__ void __launch_bounds__(256) pull_kernel(StepArgs a)
 {
-    constexpr int V = 16 / (int)sizeof(S);
+    constexpr int V = VB / (int)sizeof(S);
     const unsigned g = blockIdx.x * blockDim.x + threadIdx.x;
     double red_m = 0.0, red_e = 0.0;
 

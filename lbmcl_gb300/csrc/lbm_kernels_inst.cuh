@@ -32,6 +32,22 @@ const void *LBM_CAT(pull_kernel_ptr_, LBM_SFX)(int mode)
     }
 }
 
+cudaError_t LBM_CAT(launch_narrow_, LBM_SFX)(int mode, const StepArgs &a, unsigned grid, unsigned block,
+                                             cudaStream_t s)
+{
+    if (grid == 0) return cudaSuccess;
+    if constexpr (sizeof(LBM_S) < 8) {
+        switch (mode) {
+        case MODE_STEP: pull_kernel<LBM_S, MODE_STEP, 8><<<grid, block, 0, s>>>(a); break;
+        case MODE_STEP_MACRO: pull_kernel<LBM_S, MODE_STEP_MACRO, 8><<<grid, block, 0, s>>>(a); break;
+        default: return cudaErrorInvalidValue;
+        }
+        return cudaGetLastError();
+    } else {
+        return cudaErrorInvalidValue;  // one double per 8 bytes: no narrow variant
+    }
+}
+
 cudaError_t LBM_CAT(launch_staged_, LBM_SFX)(int mode, const StepArgs &a, unsigned grid, unsigned block,
                                              size_t smem, cudaStream_t s)
 {

@@ -21,7 +21,9 @@ struct DumpArgs;
     const void *pull_kernel_ptr_##SFX(int mode);                                                    \
     cudaError_t launch_staged_##SFX(int mode, const StepArgs &a, unsigned grid, unsigned block,      \
                                     size_t smem, cudaStream_t s);                                    \
-    const void *staged_kernel_ptr_##SFX(int mode);
+    const void *staged_kernel_ptr_##SFX(int mode);                                                  \
+    cudaError_t launch_narrow_##SFX(int mode, const StepArgs &a, unsigned grid, unsigned block,      \
+                                    cudaStream_t s);
 
 LBM_DECLARE_LAUNCHERS(f32)
 LBM_DECLARE_LAUNCHERS(f64)

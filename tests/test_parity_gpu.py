@@ -217,17 +217,18 @@ def test_deterministic_repeat(capi):
 
 @pytest.mark.parametrize("prec", ["fp32", "fp64", "fp16", "bf16"])
 @pytest.mark.parametrize("dim,stages", [(8, 2), (24, 3), (64, 0), (136, 5), (256, 0)])
-def test_staged_equals_direct(capi, prec, dim, stages):
-    """The two iteration kernels move data differently but run the same site
+def test_kernel_variants_agree(capi, prec, dim, stages):
+    """The iteration kernels move data differently but run the same site
     update: their raw population buffers agree bit for bit (incl. macros)."""
     outs = []
-    for kernel in ("direct", "staged"):
+    for kernel in ("direct", "staged", "narrow"):
         with capi.Lattice(dim, 0.005, 0.08, precision=prec, seed=21, noise_sigma=1e-4, kernel=kernel,
                           stages=stages) as L:
             L.step(7)
             L.step(6, every=6)
             L.sync()
             outs.append((L.raw(), L.rho(), L.u()))
-    np.testing.assert_array_equal(outs[0][0], outs[1][0])
-    np.testing.assert_array_equal(bits(outs[0][1]), bits(outs[1][1]))
-    np.testing.assert_array_equal(bits(outs[0][2]), bits(outs[1][2]))
+    for other in outs[1:]:
+        np.testing.assert_array_equal(outs[0][0], other[0])
+        np.testing.assert_array_equal(bits(outs[0][1]), bits(other[1]))
+        np.testing.assert_array_equal(bits(outs[0][2]), bits(other[2]))
