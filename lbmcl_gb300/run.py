@@ -22,9 +22,12 @@ def main(argv=None) -> int:
     ap.add_argument("--noise", type=float, default=1e-4)
     ap.add_argument("--seed", type=int, default=1234)
     ap.add_argument("--block", type=int, default=0)
+    ap.add_argument("--kernel", default="auto", choices=sorted(capi.KERNELS))
+    ap.add_argument("--stages", type=int, default=0)
     a = ap.parse_args(argv)
     with capi.Lattice(a.dim, a.viscosity, a.velocity, precision=a.precision, stride=0, seed=a.seed,
-                      noise_sigma=a.noise, block_threads=a.block, profile_steps=True) as L:
+                      noise_sigma=a.noise, block_threads=a.block, profile_steps=True, kernel=a.kernel,
+                      stages=a.stages) as L:
         t0 = time.perf_counter()
         L.step(a.steps, every=a.every)
         L.sync()
