@@ -119,7 +119,6 @@ struct lbm_handle {
     int kernel = LBM_KERNEL_DIRECT;
     int rows = 1, gpp = 0, stages = 0;
     unsigned ngroups = 0, sgrid = 0, sblock = 0;
-    unsigned ngrid = 0;     // narrow variant: grid over 8-byte vectors
     size_t ssmem = 0;
 };
 
@@ -249,8 +248,24 @@ int setup_staged(lbm_t *h, int want_stages)
     return LBM_OK;
 }
 
-cudaError_t launch_pull(const lbm_t *h, int mode, const lbm::StepArgs &a)
+// Split the vectors of one launch into the interior and boundary regions
+// for a thread block of `block` threads; returns the total grid.
+unsigned set_regions(lbm::StepArgs &a, unsigned block)
 {
+    const size_t m = (size_t)(a.dim - 4);
+    const size_t nvx = (size_t)a.nvx;
+    const size_t na = m * m * (nvx > 2 ? nvx - 2 : 0);
+    const size_t nb = m * m * std::min<size_t>(2, nvx) + 4 * (size_t)(a.dim - 3) * nvx;
+    a.nvec_a = (unsigned)na;
+    a.nvec_b = (unsigned)nb;
+    a.grid_a = (unsigned)((na + block - 1) / block);
+    return a.grid_a + (unsigned)((nb + block - 1) / block);
+}
+
+cudaError_t launch_pull(const lbm_t *h, int mode, const lbm::StepArgs &a0)
+{
+    lbm::StepArgs a = a0;
+    const unsigned grid = set_regions(a, h->block);
     if (h->kernel == LBM_KERNEL_STAGED && mode != lbm::MODE_REDUCE) {
         switch (h->prec) {
         case LBM_FP32: return lbm::launch_staged_f32(mode, a, h->sgrid, h->sblock, h->ssmem, h->stream);
@@ -261,20 +276,21 @@ cudaError_t launch_pull(const lbm_t *h, int mode, const lbm::StepArgs &a)
     }
     if (h->kernel == LBM_KERNEL_NARROW && mode != lbm::MODE_REDUCE) {
         // half-width vectors: twice as many threads, each owning V/2 sites
-        lbm::StepArgs n = a;
-        n.nvx = 2 * a.nvx;
-        n.nvec = 2 * a.nvec;
+        lbm::StepArgs n = a0;
+        n.nvx = 2 * a0.nvx;
+        n.nvec = 2 * a0.nvec;
+        const unsigned ngrid = set_regions(n, h->block);
         switch (h->prec) {
-        case LBM_FP32: return lbm::launch_narrow_f32(mode, n, h->ngrid, h->block, h->stream);
-        case LBM_FP16: return lbm::launch_narrow_f16(mode, n, h->ngrid, h->block, h->stream);
-        default: return lbm::launch_narrow_bf16(mode, n, h->ngrid, h->block, h->stream);
+        case LBM_FP32: return lbm::launch_narrow_f32(mode, n, ngrid, h->block, h->stream);
+        case LBM_FP16: return lbm::launch_narrow_f16(mode, n, ngrid, h->block, h->stream);
+        default: return lbm::launch_narrow_bf16(mode, n, ngrid, h->block, h->stream);
         }
     }
     switch (h->prec) {
-    case LBM_FP32: return lbm::launch_pull_f32(mode, a, h->grid, h->block, h->stream);
-    case LBM_FP64: return lbm::launch_pull_f64(mode, a, h->grid, h->block, h->stream);
-    case LBM_FP16: return lbm::launch_pull_f16(mode, a, h->grid, h->block, h->stream);
-    default: return lbm::launch_pull_bf16(mode, a, h->grid, h->block, h->stream);
+    case LBM_FP32: return lbm::launch_pull_f32(mode, a, grid, h->block, h->stream);
+    case LBM_FP64: return lbm::launch_pull_f64(mode, a, grid, h->block, h->stream);
+    case LBM_FP16: return lbm::launch_pull_f16(mode, a, grid, h->block, h->stream);
+    default: return lbm::launch_pull_bf16(mode, a, grid, h->block, h->stream);
     }
 }
 
@@ -362,7 +378,7 @@ int lbm_init(lbm_t **out, const lbm_config *c)
     const size_t fbytes = (size_t)lbm::Q * n * sb;
     const size_t stage_elems = std::min(kStageElems, (size_t)lbm::Q * n);
     const size_t need = 2 * fbytes + n + 4 * n * mb + (size_t)dim * dim * mb + stage_elems * dump_elem(prec) +
-                        (grid + 1) * 2 * sizeof(double) + 4 * sizeof(double) + sizeof(int);
+                        (grid + 2) * 2 * sizeof(double) + 4 * sizeof(double) + sizeof(int);
     if (c->max_device_bytes > 0 && need > c->max_device_bytes)
         return fail(LBM_ENOMEM, "lbm_init: needs %zu device bytes, budget is %zu", need, c->max_device_bytes);
 
@@ -404,7 +420,7 @@ int lbm_init(lbm_t **out, const lbm_config *c)
         LBM_CUDA(cudaMalloc(&h->u, 3 * n * mb));
         LBM_CUDA(cudaMalloc(&h->lid, (size_t)dim * dim * mb));
         LBM_CUDA(cudaMalloc(&h->stage, stage_elems * dump_elem(prec)));
-        LBM_CUDA(cudaMalloc((void **)&h->partials, (grid + 1) * 2 * sizeof(double)));
+        LBM_CUDA(cudaMalloc((void **)&h->partials, (grid + 2) * 2 * sizeof(double)));
         LBM_CUDA(cudaMalloc((void **)&h->red_out, 4 * sizeof(double)));
         LBM_CUDA(cudaMalloc((void **)&h->status, sizeof(int)));
         LBM_CUDA(cudaMemsetAsync(h->status, 0, sizeof(int), h->stream));
@@ -446,7 +462,6 @@ int lbm_init(lbm_t **out, const lbm_config *c)
         h->kernel = LBM_KERNEL_DIRECT;
         if (want == LBM_KERNEL_NARROW && prec != LBM_FP64) {
             h->kernel = LBM_KERNEL_NARROW;
-            h->ngrid = (unsigned)((2 * nvec + block - 1) / block);
         }
         if (want == LBM_KERNEL_STAGED) {
             const int r = setup_staged(h, c->stages);
@@ -639,8 +654,10 @@ int lbm_reduce(lbm_t *h, double out[3])
 {
     if (!h || !out) return fail(LBM_EINVAL, "lbm_reduce: NULL argument");
     const lbm::StepArgs a = step_args(h, h->cur);
+    lbm::StepArgs ra = a;
+    const unsigned rgrid = set_regions(ra, h->block);  // the grid launch_pull uses for MODE_REDUCE
     LBM_CUDA(launch_pull(h, lbm::MODE_REDUCE, a));
-    LBM_CUDA(lbm::launch_sum_partials(h->partials, (int)h->grid, h->red_out, h->stream));
+    LBM_CUDA(lbm::launch_sum_partials(h->partials, (int)rgrid, h->red_out, h->stream));
     double r[2];
     LBM_CUDA(cudaMemcpyAsync(r, h->red_out, sizeof r, cudaMemcpyDeviceToHost, h->stream));
     LBM_CUDA(cudaEventRecord(h->ev_last, h->stream));

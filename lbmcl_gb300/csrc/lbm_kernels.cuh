@@ -363,7 +363,7 @@ __device__ __forceinline__ void accumulate(const SiteOut &o, double &m, double &
 // Update the V sites x0..x0+V-1 of row (y, z) in place: fs holds their pulled
 // populations on entry and their post-collision populations on exit.  Stores
 // rho / u (MODE_STEP_MACRO) or accumulates the reduction sums (MODE_REDUCE).
-template <class S, int MODE, int V>
+template <class S, int MODE, int V, bool FLUID_ONLY = false>
 __device__ __forceinline__ void update_vector(S (&fs)[Q][V], typename MapWord<V>::type mw, const StepArgs &a,
                                               int y, int z, int x0, size_t site0, double &red_m, double &red_e)
 {
@@ -377,8 +377,27 @@ __device__ __forceinline__ void update_vector(S (&fs)[Q][V], typename MapWord<V>
     bool bad = false;
 
     const DevK K = make_devk(a.omega_f, Dev16<S>::scale, Dev16<S>::inv_scale);
+    if constexpr (!DEV) {
+        if (FLUID_ONLY) {
+#pragma unroll
+            for (int k = 0; k < V; ++k) {
+                C f[Q];
+#pragma unroll
+                for (int i = 0; i < Q; ++i) f[i] = fs[i][k];
+                SiteOut o;
+                site_exact<C, MODE != MODE_REDUCE>(f, 0, (C)0, inv_tau, W, o);
+#pragma unroll
+                for (int i = 0; i < Q; ++i) fs[i][k] = f[i];
+                bad |= o.bad;
+                if (MODE == MODE_STEP_MACRO) store_macro<C>(a, site0 + k, o);
+                if (MODE == MODE_REDUCE) accumulate(o, red_m, red_e);
+            }
+            if (bad) atomicOr(a.status, 1);
+            return;
+        }
+    }
     if constexpr (DEV) {
-        if (mw == 0) {
+        if (FLUID_ONLY || mw == 0) {
             // all V sites FLUID (the bulk of the lattice): no per-site branches,
             // two sites per step so the output converts as packed pairs
 #pragma unroll
@@ -442,34 +461,95 @@ __device__ __forceinline__ void update_vector(S (&fs)[Q][V], typename MapWord<V>
 // Direct variant: every thread loads its V sites' populations with VB-byte
 // vector loads straight from HBM (V = VB / sizeof(S)).
 // ---------------------------------------------------------------------------
+// Row / vector of the two regions of one iteration launch.
+//  interior: rows y, z in [2, dim-3], vectors 1 .. nvx-2 -- every site FLUID
+//  boundary: the first and last vector of those rows, and every vector of the
+//            rows with y or z in {1, dim-2}
+__device__ __forceinline__ void decode_interior(const StepArgs &a, unsigned g, int &xv, int &y, int &z)
+{
+    const unsigned per = (unsigned)a.nvx - 2u;
+    const unsigned row = g / per;
+    xv = 1 + (int)(g - row * per);
+    const unsigned m = (unsigned)(a.dim - 4);
+    y = 2 + (int)(row % m);
+    z = 2 + (int)(row / m);
+}
+
+__device__ __forceinline__ void decode_boundary(const StepArgs &a, unsigned g, int &xv, int &y, int &z)
+{
+    const int dim = a.dim;
+    const unsigned nvx = (unsigned)a.nvx;
+    const unsigned ends = nvx < 2u ? nvx : 2u;
+    const unsigned m = (unsigned)(dim - 4);
+    const unsigned nb1 = m * m * ends;
+    if (g < nb1) {
+        const unsigned row = g / ends;
+        const unsigned which = g - row * ends;
+        xv = which ? (int)nvx - 1 : 0;
+        y = 2 + (int)(row % m);
+        z = 2 + (int)(row / m);
+        return;
+    }
+    const unsigned g2 = g - nb1;
+    const unsigned br = g2 / nvx;
+    xv = (int)(g2 - br * nvx);
+    const unsigned side = (unsigned)(dim - 2);
+    if (br < side) {            // plane z = 1
+        z = 1;
+        y = 1 + (int)br;
+    } else if (br < 2 * side) { // plane z = dim-2
+        z = dim - 2;
+        y = 1 + (int)(br - side);
+    } else {                    // planes 2..dim-3: rows y = 1 and y = dim-2
+        const unsigned k = br - 2 * side;
+        z = 2 + (int)(k / 2);
+        y = (k & 1) ? dim - 2 : 1;
+    }
+}
+
+template <class S, int MODE, int V, bool INTERIOR>
+__device__ __forceinline__ void pull_vector(const StepArgs &a, int xv, int y, int z, double &red_m, double &red_e)
+{
+    const int dim = a.dim;
+    const int x0 = xv * V;
+    const size_t rowoff = (size_t)z * dim * dim + (size_t)y * dim;
+    const size_t site0 = rowoff + (size_t)x0;
+    typename MapWord<V>::type mw = 0;
+    if (!INTERIOR) mw = __ldg(reinterpret_cast<const typename MapWord<V>::type *>(a.map + site0));
+    const S *__restrict__ fin = static_cast<const S *>(a.fin);
+    S fs[Q][V];
+    gather_all<S, V, 0>(fin, a.n, rowoff, dim, x0, fs);
+    update_vector<S, MODE, V, INTERIOR>(fs, mw, a, y, z, x0, site0, red_m, red_e);
+    if (MODE != MODE_REDUCE) {
+        S *__restrict__ fout = static_cast<S *>(a.fout);
+#pragma unroll
+        for (int i = 0; i < Q; ++i) store_vec<S, V>(fout + (size_t)i * a.n + site0, fs[i]);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Direct variant: every thread loads its V sites' populations with VB-byte
+// vector loads straight from HBM (V = VB / sizeof(S)).  Blocks [0, grid_a)
+// take interior vectors (branch-free FLUID path, no map read), the others the
+// boundary vectors, so no warp mixes the two paths.
+// ---------------------------------------------------------------------------
 template <class S, int MODE, int VB = 16>
 __global__ void __launch_bounds__(256) pull_kernel(StepArgs a)
 {
     constexpr int V = VB / (int)sizeof(S);
-    const unsigned g = blockIdx.x * blockDim.x + threadIdx.x;
     double red_m = 0.0, red_e = 0.0;
-
-    if (g < a.nvec) {
-        const int dim = a.dim;
-        const unsigned xv = g % (unsigned)a.nvx;
-        const unsigned row = g / (unsigned)a.nvx;
-        const int y = 1 + (int)(row % (unsigned)(dim - 2));
-        const int z = 1 + (int)(row / (unsigned)(dim - 2));
-        const int x0 = (int)xv * V;
-        const size_t rowoff = (size_t)z * dim * dim + (size_t)y * dim;
-        const size_t site0 = rowoff + (size_t)x0;
-
-        const typename MapWord<V>::type mw =
-            __ldg(reinterpret_cast<const typename MapWord<V>::type *>(a.map + site0));
-        const S *__restrict__ fin = static_cast<const S *>(a.fin);
-        S fs[Q][V];
-        gather_all<S, V, 0>(fin, a.n, rowoff, dim, x0, fs);
-        update_vector<S, MODE, V>(fs, mw, a, y, z, x0, site0, red_m, red_e);
-
-        if (MODE != MODE_REDUCE) {
-            S *__restrict__ fout = static_cast<S *>(a.fout);
-#pragma unroll
-            for (int i = 0; i < Q; ++i) store_vec<S, V>(fout + (size_t)i * a.n + site0, fs[i]);
+    int xv, y, z;
+    if (blockIdx.x < a.grid_a) {
+        const unsigned g = blockIdx.x * blockDim.x + threadIdx.x;
+        if (g < a.nvec_a) {
+            decode_interior(a, g, xv, y, z);
+            pull_vector<S, MODE, V, true>(a, xv, y, z, red_m, red_e);
+        }
+    } else {
+        const unsigned g = (blockIdx.x - a.grid_a) * blockDim.x + threadIdx.x;
+        if (g < a.nvec_b) {
+            decode_boundary(a, g, xv, y, z);
+            pull_vector<S, MODE, V, false>(a, xv, y, z, red_m, red_e);
         }
     }
     if (MODE == MODE_REDUCE) block_reduce_write(red_m, red_e, a.partials);
