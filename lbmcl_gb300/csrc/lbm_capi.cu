@@ -248,24 +248,8 @@ int setup_staged(lbm_t *h, int want_stages)
     return LBM_OK;
 }
 
-// Split the vectors of one launch into the interior and boundary regions
-// for a thread block of `block` threads; returns the total grid.
-unsigned set_regions(lbm::StepArgs &a, unsigned block)
+cudaError_t launch_pull(const lbm_t *h, int mode, const lbm::StepArgs &a, unsigned *nparts = nullptr)
 {
-    const size_t m = (size_t)(a.dim - 4);
-    const size_t nvx = (size_t)a.nvx;
-    const size_t na = m * m * (nvx > 2 ? nvx - 2 : 0);
-    const size_t nb = m * m * std::min<size_t>(2, nvx) + 4 * (size_t)(a.dim - 3) * nvx;
-    a.nvec_a = (unsigned)na;
-    a.nvec_b = (unsigned)nb;
-    a.grid_a = (unsigned)((na + block - 1) / block);
-    return a.grid_a + (unsigned)((nb + block - 1) / block);
-}
-
-cudaError_t launch_pull(const lbm_t *h, int mode, const lbm::StepArgs &a0)
-{
-    lbm::StepArgs a = a0;
-    const unsigned grid = set_regions(a, h->block);
     if (h->kernel == LBM_KERNEL_STAGED && mode != lbm::MODE_REDUCE) {
         switch (h->prec) {
         case LBM_FP32: return lbm::launch_staged_f32(mode, a, h->sgrid, h->sblock, h->ssmem, h->stream);
@@ -275,22 +259,17 @@ cudaError_t launch_pull(const lbm_t *h, int mode, const lbm::StepArgs &a0)
         }
     }
     if (h->kernel == LBM_KERNEL_NARROW && mode != lbm::MODE_REDUCE) {
-        // half-width vectors: twice as many threads, each owning V/2 sites
-        lbm::StepArgs n = a0;
-        n.nvx = 2 * a0.nvx;
-        n.nvec = 2 * a0.nvec;
-        const unsigned ngrid = set_regions(n, h->block);
         switch (h->prec) {
-        case LBM_FP32: return lbm::launch_narrow_f32(mode, n, ngrid, h->block, h->stream);
-        case LBM_FP16: return lbm::launch_narrow_f16(mode, n, ngrid, h->block, h->stream);
-        default: return lbm::launch_narrow_bf16(mode, n, ngrid, h->block, h->stream);
+        case LBM_FP32: return lbm::launch_narrow_f32(mode, a, h->block, h->stream);
+        case LBM_FP16: return lbm::launch_narrow_f16(mode, a, h->block, h->stream);
+        default: return lbm::launch_narrow_bf16(mode, a, h->block, h->stream);
         }
     }
     switch (h->prec) {
-    case LBM_FP32: return lbm::launch_pull_f32(mode, a, grid, h->block, h->stream);
-    case LBM_FP64: return lbm::launch_pull_f64(mode, a, grid, h->block, h->stream);
-    case LBM_FP16: return lbm::launch_pull_f16(mode, a, grid, h->block, h->stream);
-    default: return lbm::launch_pull_bf16(mode, a, grid, h->block, h->stream);
+    case LBM_FP32: return lbm::launch_pull_f32(mode, a, h->block, h->stream, nparts);
+    case LBM_FP64: return lbm::launch_pull_f64(mode, a, h->block, h->stream, nparts);
+    case LBM_FP16: return lbm::launch_pull_f16(mode, a, h->block, h->stream, nparts);
+    default: return lbm::launch_pull_bf16(mode, a, h->block, h->stream, nparts);
     }
 }
 
@@ -654,10 +633,9 @@ int lbm_reduce(lbm_t *h, double out[3])
 {
     if (!h || !out) return fail(LBM_EINVAL, "lbm_reduce: NULL argument");
     const lbm::StepArgs a = step_args(h, h->cur);
-    lbm::StepArgs ra = a;
-    const unsigned rgrid = set_regions(ra, h->block);  // the grid launch_pull uses for MODE_REDUCE
-    LBM_CUDA(launch_pull(h, lbm::MODE_REDUCE, a));
-    LBM_CUDA(lbm::launch_sum_partials(h->partials, (int)rgrid, h->red_out, h->stream));
+    unsigned nparts = 0;
+    LBM_CUDA(launch_pull(h, lbm::MODE_REDUCE, a, &nparts));
+    LBM_CUDA(lbm::launch_sum_partials(h->partials, (int)nparts, h->red_out, h->stream));
     double r[2];
     LBM_CUDA(cudaMemcpyAsync(r, h->red_out, sizeof r, cudaMemcpyDeviceToHost, h->stream));
     LBM_CUDA(cudaEventRecord(h->ev_last, h->stream));

@@ -306,9 +306,7 @@ struct StepArgs {
     int dim;
     int nvx;             // x-vectors per row = dim / V
     unsigned nvec;       // vectors in the interior rows = nvx * (dim-2)^2
-    unsigned nvec_a;     // interior-region vectors (all sites FLUID)
-    unsigned nvec_b;     // boundary-region vectors
-    unsigned grid_a;     // blocks of the interior region (the boundary blocks follow)
+    unsigned partial_base;  // first reduction-partial slot of this launch
     size_t n;            // dim^3
     double inv_tau;      // 1/tau in the compute precision (rounded by the host)
     float omega_f;       // 1/tau as float, deviation kernels

@@ -311,7 +311,8 @@ __device__ __forceinline__ void site_dev(float (&D)[Q], uint8_t b, float lidv, c
     }
 }
 
-// Block reduction of (mass, energy) in double, written to partials[2*block].
+// Block reduction of (mass, energy) in double, written to partials[2*block]
+// (partials already offset by the launch's first block).
 __device__ __forceinline__ void block_reduce_write(double m, double e, double *partials)
 {
     // warp shuffles: the reductions are the only place this code uses them
@@ -388,9 +389,12 @@ __device__ __forceinline__ void update_vector(S (&fs)[Q][V], typename MapWord<V>
                 site_exact<C, MODE != MODE_REDUCE>(f, 0, (C)0, inv_tau, W, o);
 #pragma unroll
                 for (int i = 0; i < Q; ++i) fs[i][k] = f[i];
-                bad |= o.bad;
-                if (MODE == MODE_STEP_MACRO) store_macro<C>(a, site0 + k, o);
-                if (MODE == MODE_REDUCE) accumulate(o, red_m, red_e);
+                // x in [2, dim-3] is FLUID; the row ends are walls / faces
+                if ((unsigned)(x0 + k - 2) <= (unsigned)(dim - 5)) {
+                    bad |= o.bad;
+                    if (MODE == MODE_STEP_MACRO) store_macro<C>(a, site0 + k, o);
+                    if (MODE == MODE_REDUCE) accumulate(o, red_m, red_e);
+                }
             }
             if (bad) atomicOr(a.status, 1);
             return;
@@ -411,18 +415,21 @@ __device__ __forceinline__ void update_vector(S (&fs)[Q][V], typename MapWord<V>
                 SiteOut o0, o1;
                 fluid_dev<MODE != MODE_REDUCE>(D0, K, o0);
                 fluid_dev<MODE != MODE_REDUCE>(D1, K, o1);
-                bad |= o0.bad | o1.bad;
                 if (MODE != MODE_REDUCE) {
 #pragma unroll
                     for (int i = 0; i < Q; ++i) Dev16<S>::from_f2(D0[i], D1[i], fs[i][k], fs[i][k + 1]);
                 }
+                // in an interior row, x in [2, dim-3] is FLUID; the row ends are walls / faces
+                const bool f0 = !FLUID_ONLY || (unsigned)(x0 + k - 2) <= (unsigned)(dim - 5);
+                const bool f1 = !FLUID_ONLY || (unsigned)(x0 + k - 1) <= (unsigned)(dim - 5);
+                bad |= (f0 && o0.bad) || (f1 && o1.bad);
                 if (MODE == MODE_STEP_MACRO) {
-                    store_macro<C>(a, site0 + k, o0);
-                    store_macro<C>(a, site0 + k + 1, o1);
+                    if (f0) store_macro<C>(a, site0 + k, o0);
+                    if (f1) store_macro<C>(a, site0 + k + 1, o1);
                 }
                 if (MODE == MODE_REDUCE) {
-                    accumulate(o0, red_m, red_e);
-                    accumulate(o1, red_m, red_e);
+                    if (f0) accumulate(o0, red_m, red_e);
+                    if (f1) accumulate(o1, red_m, red_e);
                 }
             }
             if (bad) atomicOr(a.status, 1);
@@ -457,53 +464,32 @@ __device__ __forceinline__ void update_vector(S (&fs)[Q][V], typename MapWord<V>
     if (bad) atomicOr(a.status, 1);
 }
 
-// ---------------------------------------------------------------------------
-// Direct variant: every thread loads its V sites' populations with VB-byte
-// vector loads straight from HBM (V = VB / sizeof(S)).
-// ---------------------------------------------------------------------------
-// Row / vector of the two regions of one iteration launch.
-//  interior: rows y, z in [2, dim-3], vectors 1 .. nvx-2 -- every site FLUID
-//  boundary: the first and last vector of those rows, and every vector of the
-//            rows with y or z in {1, dim-2}
-__device__ __forceinline__ void decode_interior(const StepArgs &a, unsigned g, int &xv, int &y, int &z)
+// Bounce-back of the x-face site x = xf of an interior row (y, z in
+// [2, dim-3]): its output population i is its pulled input of the opposite
+// direction, and an input whose source is the wall (x = 0 or dim-1) is the
+// site's initial equilibrium w_i (kernels.cl:400-408 with the fixed
+// wall-sourced slots; interior rows are never on the lid).  Reloaded from
+// the input buffer, so the interior fast path can run on every lane first.
+template <class S, int V>
+__device__ __forceinline__ void face_fix(const StepArgs &a, size_t rowoff, int xf, int k, S (&fs)[Q][V])
 {
-    const unsigned per = (unsigned)a.nvx - 2u;
-    const unsigned row = g / per;
-    xv = 1 + (int)(g - row * per);
-    const unsigned m = (unsigned)(a.dim - 4);
-    y = 2 + (int)(row % m);
-    z = 2 + (int)(row / m);
-}
-
-__device__ __forceinline__ void decode_boundary(const StepArgs &a, unsigned g, int &xv, int &y, int &z)
-{
+    using C = typename Compute<S>::type;
+    const S *__restrict__ fin = static_cast<const S *>(a.fin);
     const int dim = a.dim;
-    const unsigned nvx = (unsigned)a.nvx;
-    const unsigned ends = nvx < 2u ? nvx : 2u;
-    const unsigned m = (unsigned)(dim - 4);
-    const unsigned nb1 = m * m * ends;
-    if (g < nb1) {
-        const unsigned row = g / ends;
-        const unsigned which = g - row * ends;
-        xv = which ? (int)nvx - 1 : 0;
-        y = 2 + (int)(row % m);
-        z = 2 + (int)(row / m);
-        return;
-    }
-    const unsigned g2 = g - nb1;
-    const unsigned br = g2 / nvx;
-    xv = (int)(g2 - br * nvx);
-    const unsigned side = (unsigned)(dim - 2);
-    if (br < side) {            // plane z = 1
-        z = 1;
-        y = 1 + (int)br;
-    } else if (br < 2 * side) { // plane z = dim-2
-        z = dim - 2;
-        y = 1 + (int)(br - side);
-    } else {                    // planes 2..dim-3: rows y = 1 and y = dim-2
-        const unsigned k = br - 2 * side;
-        z = 2 + (int)(k / 2);
-        y = (k & 1) ? dim - 2 : 1;
+    const Weights<C> W = make_weights<C>();
+#pragma unroll
+    for (int i = 0; i < Q; ++i) {
+        const int j = opp_of(i);
+        const int sx = xf - ex_of(j);
+        S v;
+        if (sx == 0 || sx == dim - 1) {
+            if constexpr (is_dev16<S>()) v = zero_elem<S>();
+            else v = (S)W.w[wclass_of(j)];
+        } else {
+            const ptrdiff_t shift = (ptrdiff_t)ez_of(j) * dim * dim + (ptrdiff_t)ey_of(j) * dim;
+            v = load_one(fin + (size_t)j * a.n + rowoff - shift + sx);
+        }
+        fs[i][k] = v;
     }
 }
 
@@ -520,6 +506,11 @@ __device__ __forceinline__ void pull_vector(const StepArgs &a, int xv, int y, in
     S fs[Q][V];
     gather_all<S, V, 0>(fin, a.n, rowoff, dim, x0, fs);
     update_vector<S, MODE, V, INTERIOR>(fs, mw, a, y, z, x0, site0, red_m, red_e);
+    if (INTERIOR && MODE != MODE_REDUCE) {
+        // the walls (x = 0, dim-1) hold values nobody reads; the faces bounce back
+        if (x0 == 0) face_fix<S, V>(a, rowoff, 1, 1, fs);
+        if (x0 + V == dim) face_fix<S, V>(a, rowoff, dim - 2, V - 2, fs);
+    }
     if (MODE != MODE_REDUCE) {
         S *__restrict__ fout = static_cast<S *>(a.fout);
 #pragma unroll
@@ -529,30 +520,58 @@ __device__ __forceinline__ void pull_vector(const StepArgs &a, int xv, int y, in
 
 // ---------------------------------------------------------------------------
 // Direct variant: every thread loads its V sites' populations with VB-byte
-// vector loads straight from HBM (V = VB / sizeof(S)).  Blocks [0, grid_a)
-// take interior vectors (branch-free FLUID path, no map read), the others the
-// boundary vectors, so no warp mixes the two paths.
+// vector loads straight from HBM (V = VB / sizeof(S)).  One iteration is two
+// launches over disjoint sets of whole rows:
+//   ROWS_INTERIOR  the (dim-4)^2 rows with y, z in [2, dim-3]: branch-free
+//                  FLUID update on every lane, the two x-face sites of each
+//                  row patched afterwards by face_fix (no map read)
+//   ROWS_FACES     the 4 (dim-3) rows with y or z in {1, dim-2}: the general,
+//                  map-driven site update
+// Each launch gets its own register allocation, and rows stay whole, so no
+// 32-byte sector is shared between the two launches.
 // ---------------------------------------------------------------------------
-template <class S, int MODE, int VB = 16>
-__global__ void __launch_bounds__(256) pull_kernel(StepArgs a)
+enum { ROWS_INTERIOR = 0, ROWS_FACES = 1 };
+
+// face row index -> (y, z): plane z = 1, plane z = dim-2, then rows y = 1 and
+// y = dim-2 of the planes 2 .. dim-3
+__device__ __forceinline__ void decode_face_row(int dim, unsigned br, int &y, int &z)
+{
+    const unsigned side = (unsigned)(dim - 2);
+    if (br < side) {
+        z = 1;
+        y = 1 + (int)br;
+    } else if (br < 2 * side) {
+        z = dim - 2;
+        y = 1 + (int)(br - side);
+    } else {
+        const unsigned k = br - 2 * side;
+        z = 2 + (int)(k / 2);
+        y = (k & 1) ? dim - 2 : 1;
+    }
+}
+
+template <class S, int MODE, int VB, int ROWS>
+__global__ void __launch_bounds__(256, 2) pull_kernel(StepArgs a)
 {
     constexpr int V = VB / (int)sizeof(S);
+    const unsigned g = blockIdx.x * blockDim.x + threadIdx.x;
     double red_m = 0.0, red_e = 0.0;
-    int xv, y, z;
-    if (blockIdx.x < a.grid_a) {
-        const unsigned g = blockIdx.x * blockDim.x + threadIdx.x;
-        if (g < a.nvec_a) {
-            decode_interior(a, g, xv, y, z);
-            pull_vector<S, MODE, V, true>(a, xv, y, z, red_m, red_e);
+    const unsigned nrows = ROWS == ROWS_INTERIOR ? (unsigned)(a.dim - 4) * (unsigned)(a.dim - 4)
+                                                 : 4u * (unsigned)(a.dim - 3);
+    if (g < nrows * (unsigned)a.nvx) {
+        const int dim = a.dim;
+        const unsigned row = g / (unsigned)a.nvx;
+        const int xv = (int)(g - row * (unsigned)a.nvx);
+        int y, z;
+        if (ROWS == ROWS_INTERIOR) {
+            y = 2 + (int)(row % (unsigned)(dim - 4));
+            z = 2 + (int)(row / (unsigned)(dim - 4));
+        } else {
+            decode_face_row(dim, row, y, z);
         }
-    } else {
-        const unsigned g = (blockIdx.x - a.grid_a) * blockDim.x + threadIdx.x;
-        if (g < a.nvec_b) {
-            decode_boundary(a, g, xv, y, z);
-            pull_vector<S, MODE, V, false>(a, xv, y, z, red_m, red_e);
-        }
+        pull_vector<S, MODE, V, ROWS == ROWS_INTERIOR>(a, xv, y, z, red_m, red_e);
     }
-    if (MODE == MODE_REDUCE) block_reduce_write(red_m, red_e, a.partials);
+    if (MODE == MODE_REDUCE) block_reduce_write(red_m, red_e, a.partials + 2 * (size_t)a.partial_base);
 }
 
 // ---------------------------------------------------------------------------

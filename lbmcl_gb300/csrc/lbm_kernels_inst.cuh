@@ -9,40 +9,57 @@ namespace lbm {
 #define LBM_CAT2(a, b) a##b
 #define LBM_CAT(a, b) LBM_CAT2(a, b)
 
-cudaError_t LBM_CAT(launch_pull_, LBM_SFX)(int mode, const StepArgs &a, unsigned grid, unsigned block,
-                                           cudaStream_t s)
+// One iteration (or reduction pass) of the direct variant with VB-byte
+// vectors: the interior-row launch, then the face-row launch.  *nparts gets
+// the number of reduction partial slots the two launches use.
+template <int VB>
+static cudaError_t launch_direct(int mode, const StepArgs &a0, unsigned block, cudaStream_t s, unsigned *nparts)
 {
-    if (grid == 0) return cudaSuccess;
-    switch (mode) {
-    case MODE_STEP: pull_kernel<LBM_S, MODE_STEP><<<grid, block, 0, s>>>(a); break;
-    case MODE_STEP_MACRO: pull_kernel<LBM_S, MODE_STEP_MACRO><<<grid, block, 0, s>>>(a); break;
-    case MODE_REDUCE: pull_kernel<LBM_S, MODE_REDUCE><<<grid, block, 0, s>>>(a); break;
-    default: return cudaErrorInvalidValue;
-    }
-    return cudaGetLastError();
-}
-
-const void *LBM_CAT(pull_kernel_ptr_, LBM_SFX)(int mode)
-{
-    switch (mode) {
-    case MODE_STEP: return (const void *)pull_kernel<LBM_S, MODE_STEP>;
-    case MODE_STEP_MACRO: return (const void *)pull_kernel<LBM_S, MODE_STEP_MACRO>;
-    case MODE_REDUCE: return (const void *)pull_kernel<LBM_S, MODE_REDUCE>;
-    default: return nullptr;
-    }
-}
-
-cudaError_t LBM_CAT(launch_narrow_, LBM_SFX)(int mode, const StepArgs &a, unsigned grid, unsigned block,
-                                             cudaStream_t s)
-{
-    if (grid == 0) return cudaSuccess;
-    if constexpr (sizeof(LBM_S) < 8) {
-        switch (mode) {
-        case MODE_STEP: pull_kernel<LBM_S, MODE_STEP, 8><<<grid, block, 0, s>>>(a); break;
-        case MODE_STEP_MACRO: pull_kernel<LBM_S, MODE_STEP_MACRO, 8><<<grid, block, 0, s>>>(a); break;
-        default: return cudaErrorInvalidValue;
+    constexpr int V = VB / (int)sizeof(LBM_S);
+    StepArgs a = a0;
+    a.nvx = a0.dim / V;
+    const size_t m = (size_t)(a.dim - 4);
+    const unsigned gi = (unsigned)((m * m * (size_t)a.nvx + block - 1) / block);
+    const unsigned gf = (unsigned)(((size_t)4 * (a.dim - 3) * (size_t)a.nvx + block - 1) / block);
+    for (int pass = 0; pass < 2; ++pass) {
+        const unsigned grid = pass == 0 ? gi : gf;
+        if (grid == 0) continue;
+        a.partial_base = pass == 0 ? 0u : gi;
+        if (pass == 0) {
+            switch (mode) {
+            case MODE_STEP: pull_kernel<LBM_S, MODE_STEP, VB, ROWS_INTERIOR><<<grid, block, 0, s>>>(a); break;
+            case MODE_STEP_MACRO:
+                pull_kernel<LBM_S, MODE_STEP_MACRO, VB, ROWS_INTERIOR><<<grid, block, 0, s>>>(a);
+                break;
+            case MODE_REDUCE: pull_kernel<LBM_S, MODE_REDUCE, VB, ROWS_INTERIOR><<<grid, block, 0, s>>>(a); break;
+            default: return cudaErrorInvalidValue;
+            }
+        } else {
+            switch (mode) {
+            case MODE_STEP: pull_kernel<LBM_S, MODE_STEP, VB, ROWS_FACES><<<grid, block, 0, s>>>(a); break;
+            case MODE_STEP_MACRO: pull_kernel<LBM_S, MODE_STEP_MACRO, VB, ROWS_FACES><<<grid, block, 0, s>>>(a); break;
+            case MODE_REDUCE: pull_kernel<LBM_S, MODE_REDUCE, VB, ROWS_FACES><<<grid, block, 0, s>>>(a); break;
+            default: return cudaErrorInvalidValue;
+            }
         }
-        return cudaGetLastError();
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    if (nparts) *nparts = gi + gf;
+    return cudaSuccess;
+}
+
+cudaError_t LBM_CAT(launch_pull_, LBM_SFX)(int mode, const StepArgs &a, unsigned block, cudaStream_t s,
+                                           unsigned *nparts)
+{
+    return launch_direct<16>(mode, a, block, s, nparts);
+}
+
+cudaError_t LBM_CAT(launch_narrow_, LBM_SFX)(int mode, const StepArgs &a, unsigned block, cudaStream_t s)
+{
+    if constexpr (sizeof(LBM_S) < 8) {
+        if (mode == MODE_REDUCE) return cudaErrorInvalidValue;
+        return launch_direct<8>(mode, a, block, s, nullptr);
     } else {
         return cudaErrorInvalidValue;  // one double per 8 bytes: no narrow variant
     }

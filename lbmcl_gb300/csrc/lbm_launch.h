@@ -13,17 +13,15 @@ struct DumpArgs;
 
 // prec: 0 FP32, 1 FP64, 2 FP16, 3 BF16 (lbm_precision)
 #define LBM_DECLARE_LAUNCHERS(SFX)                                                                   \
-    cudaError_t launch_pull_##SFX(int mode, const StepArgs &a, unsigned grid, unsigned block,        \
-                                  cudaStream_t s);                                                   \
-    cudaError_t launch_init_##SFX(const InitArgs &a, cudaStream_t s);                               \
-    cudaError_t launch_dump_##SFX(const DumpArgs &a, cudaStream_t s);                               \
-    cudaError_t launch_load_##SFX(const DumpArgs &a, cudaStream_t s);                               \
-    const void *pull_kernel_ptr_##SFX(int mode);                                                    \
+    cudaError_t launch_pull_##SFX(int mode, const StepArgs &a, unsigned block, cudaStream_t s,       \
+                                  unsigned *nparts);                                                 \
+    cudaError_t launch_narrow_##SFX(int mode, const StepArgs &a, unsigned block, cudaStream_t s);    \
     cudaError_t launch_staged_##SFX(int mode, const StepArgs &a, unsigned grid, unsigned block,      \
                                     size_t smem, cudaStream_t s);                                    \
     const void *staged_kernel_ptr_##SFX(int mode);                                                  \
-    cudaError_t launch_narrow_##SFX(int mode, const StepArgs &a, unsigned grid, unsigned block,      \
-                                    cudaStream_t s);
+    cudaError_t launch_init_##SFX(const InitArgs &a, cudaStream_t s);                               \
+    cudaError_t launch_dump_##SFX(const DumpArgs &a, cudaStream_t s);                               \
+    cudaError_t launch_load_##SFX(const DumpArgs &a, cudaStream_t s);
 
 LBM_DECLARE_LAUNCHERS(f32)
 LBM_DECLARE_LAUNCHERS(f64)
