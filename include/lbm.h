@@ -65,7 +65,8 @@ typedef enum lbm_what {
     LBM_DUMP_U = 2,       /* velocity, planar ux,uy,uz: 3*dim^3 values (kernels.cl:68-70) */
     LBM_DUMP_MAP = 3,     /* reference cell types as int32 (common.h:7-20): dim^3 values  */
     LBM_DUMP_MAP_U8 = 4,  /* the packed byte map the kernels read: dim^3 bytes            */
-    LBM_DUMP_F_RAW = 5    /* the raw internal population buffer (binary checkpoint)       */
+    LBM_DUMP_F_RAW = 5    /* the raw internal population buffer (binary checkpoint); the
+                             slots of wall sites hold unspecified values                  */
 } lbm_what;
 
 typedef struct lbm_config {

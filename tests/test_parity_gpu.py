@@ -219,7 +219,7 @@ def test_deterministic_repeat(capi):
 @pytest.mark.parametrize("dim,stages", [(8, 2), (24, 3), (64, 0), (136, 5), (256, 0)])
 def test_kernel_variants_agree(capi, prec, dim, stages):
     """The iteration kernels move data differently but run the same site
-    update: their raw population buffers agree bit for bit (incl. macros)."""
+    update: their populations and macros agree bit for bit."""
     outs = []
     for kernel in ("direct", "staged", "narrow"):
         with capi.Lattice(dim, 0.005, 0.08, precision=prec, seed=21, noise_sigma=1e-4, kernel=kernel,
@@ -227,8 +227,10 @@ def test_kernel_variants_agree(capi, prec, dim, stages):
             L.step(7)
             L.step(6, every=6)
             L.sync()
-            outs.append((L.raw(), L.rho(), L.u()))
+            outs.append((L.f(), L.rho(), L.u()))
+    # the F view; the raw buffers may differ at wall sites, whose slots no
+    # iteration or dump ever reads
     for other in outs[1:]:
-        np.testing.assert_array_equal(outs[0][0], other[0])
+        np.testing.assert_array_equal(bits(outs[0][0]), bits(other[0]))
         np.testing.assert_array_equal(bits(outs[0][1]), bits(other[1]))
         np.testing.assert_array_equal(bits(outs[0][2]), bits(other[2]))
