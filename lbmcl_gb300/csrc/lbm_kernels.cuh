@@ -550,8 +550,25 @@ __device__ __forceinline__ void decode_face_row(int dim, unsigned br, int &y, in
     }
 }
 
+// Minimum resident 256-thread blocks per SM the direct kernels are compiled
+// for, i.e. their register cap (65536 / (256 * n)): 2 (128 registers) for the
+// 16-bit kernels, none for the exact FP32 / FP64 kernels.
+#ifndef LBM_MINB_16
+#define LBM_MINB_16 2
+#endif
+#ifndef LBM_MINB_32
+#define LBM_MINB_32 1
+#endif
+#ifndef LBM_MINB_64
+#define LBM_MINB_64 1
+#endif
+template <class S> constexpr int min_blocks()
+{
+    return sizeof(S) == 2 ? LBM_MINB_16 : (sizeof(S) == 4 ? LBM_MINB_32 : LBM_MINB_64);
+}
+
 template <class S, int MODE, int VB, int ROWS>
-__global__ void __launch_bounds__(256, 2) pull_kernel(StepArgs a)
+__global__ void __launch_bounds__(256, min_blocks<S>()) pull_kernel(StepArgs a)
 {
     constexpr int V = VB / (int)sizeof(S);
     const unsigned g = blockIdx.x * blockDim.x + threadIdx.x;
