@@ -89,7 +89,8 @@ typedef struct lbm_config {
     int device;                /* CUDA device ordinal                                       */
     int profile_steps;         /* 1: one CUDA event pair per iteration (reference's
                                   per-kernel events); 0: one pair per lbm_step call         */
-    int kernel;                /* lbm_kernel: iteration kernel variant; 0 = tuned default  */
+    int kernel;                /* lbm_kernel: iteration kernel variant; 0 = the tuned default
+                                  (NARROW for FP32, DIRECT otherwise)                       */
     int stages;                /* TMA-staged kernel: pipeline depth (0 = tuned default)    */
 } lbm_config;
 

@@ -435,9 +435,10 @@ int lbm_init(lbm_t **out, const lbm_config *c)
         // the copy source (lidh) must outlive the copy
         LBM_CUDA(cudaStreamSynchronize(h->stream));
 
-        // iteration kernel: 16-bit storage defaults to the staged variant
+        // iteration kernel: the fastest variant measured at 512^3 on GB300 --
+        // 16-byte vectors for 16-bit storage and FP64, 8-byte vectors for FP32
         int want = c->kernel;
-        if (want == LBM_KERNEL_AUTO) want = (prec == LBM_FP16 || prec == LBM_BF16) ? LBM_KERNEL_STAGED : LBM_KERNEL_DIRECT;
+        if (want == LBM_KERNEL_AUTO) want = prec == LBM_FP32 ? LBM_KERNEL_NARROW : LBM_KERNEL_DIRECT;
         h->kernel = LBM_KERNEL_DIRECT;
         if (want == LBM_KERNEL_NARROW && prec != LBM_FP64) {
             h->kernel = LBM_KERNEL_NARROW;

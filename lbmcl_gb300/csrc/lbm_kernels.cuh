@@ -550,25 +550,32 @@ __device__ __forceinline__ void decode_face_row(int dim, unsigned br, int &y, in
     }
 }
 
-// Minimum resident 256-thread blocks per SM the direct kernels are compiled
-// for, i.e. their register cap (65536 / (256 * n)): 2 (128 registers) for the
-// 16-bit kernels, none for the exact FP32 / FP64 kernels.
+// Minimum resident 256-thread blocks per SM each direct kernel is compiled
+// for, i.e. its register cap 65536 / (256 n).  Measured at 512^3 on GB300:
+// 16-bit storage runs fastest at 128 registers (n = 2) with either vector
+// width, FP32 with 8-byte vectors at 85 (n = 3); FP64 is FP64-throughput bound
+// and left uncapped.
 #ifndef LBM_MINB_16
 #define LBM_MINB_16 2
 #endif
-#ifndef LBM_MINB_32
-#define LBM_MINB_32 1
+#ifndef LBM_MINB_32_V16
+#define LBM_MINB_32_V16 2
+#endif
+#ifndef LBM_MINB_32_V8
+#define LBM_MINB_32_V8 3
 #endif
 #ifndef LBM_MINB_64
 #define LBM_MINB_64 1
 #endif
-template <class S> constexpr int min_blocks()
+template <class S, int VB> constexpr int min_blocks()
 {
-    return sizeof(S) == 2 ? LBM_MINB_16 : (sizeof(S) == 4 ? LBM_MINB_32 : LBM_MINB_64);
+    return sizeof(S) == 2 ? LBM_MINB_16
+         : sizeof(S) == 4 ? (VB == 16 ? LBM_MINB_32_V16 : LBM_MINB_32_V8)
+                          : LBM_MINB_64;
 }
 
 template <class S, int MODE, int VB, int ROWS>
-__global__ void __launch_bounds__(256, min_blocks<S>()) pull_kernel(StepArgs a)
+__global__ void __launch_bounds__(256, min_blocks<S, VB>()) pull_kernel(StepArgs a)
 {
     constexpr int V = VB / (int)sizeof(S);
     const unsigned g = blockIdx.x * blockDim.x + threadIdx.x;
