@@ -342,11 +342,16 @@ def main():
             if "fp16" in res and "fp32" in res else None,
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
-                         "traffic": traffic, "algorithmic_bytes_per_launch": wet * BYTES_PER_SITE[head]},
+                         "kernel": "pull_kernel, one iteration = interior-row launch + face-row launch",
+                         "algorithmic_bytes_per_iteration": wet * BYTES_PER_SITE[head],
+                         "traffic": traffic,
+                         "traffic_kernel": "interior-row launch (99.2% of the iteration's bytes), ncu DRAM "
+                                           "read+write at 256^3 scaled by units to 512^3",
+                         "traffic_launch_algorithmic_bytes": (dim - 4) ** 2 * (dim - 2) * BYTES_PER_SITE[head]},
             "e2e": {"value": round(e2e_mlups, 1), "unit": "MLUPS", "h2d_bytes_per_step": h2d / args.steps,
                     "d2h_bytes_per_step": d2h / args.steps,
                     "what": "lbm_init (host config + lid profile) + K iterations + rho/u read-back to pinned host"},
-            "gpu_launches": args.steps,
+            "gpu_launches": 2 * args.steps,
             "clocks": sampler.summary(),
             "cpu_baseline": cpu,
         }

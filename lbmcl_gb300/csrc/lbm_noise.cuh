@@ -52,9 +52,13 @@ __device__ __forceinline__ double series_log(double x)
     }
     const double s = __ddiv_rn(__dsub_rn(m, 1.0), __dadd_rn(m, 1.0));
     const double s2 = __dmul_rn(s, s);
-    double acc = __ddiv_rn(1.0, 23.0);
+    // 1 / (2k + 1), k = 0 .. 11, folded at compile time to the correctly
+    // rounded doubles (the values an IEEE division yields at run time)
+    constexpr double inv_odd[12] = {1.0 / 1.0,  1.0 / 3.0,  1.0 / 5.0,  1.0 / 7.0,  1.0 / 9.0,  1.0 / 11.0,
+                                    1.0 / 13.0, 1.0 / 15.0, 1.0 / 17.0, 1.0 / 19.0, 1.0 / 21.0, 1.0 / 23.0};
+    double acc = inv_odd[11];
 #pragma unroll
-    for (int k = 10; k >= 0; --k) acc = __dadd_rn(__ddiv_rn(1.0, (double)(2 * k + 1)), __dmul_rn(s2, acc));
+    for (int k = 10; k >= 0; --k) acc = __dadd_rn(inv_odd[k], __dmul_rn(s2, acc));
     const double ln2 = 0.6931471805599453;
     return __dadd_rn(__dmul_rn((double)e, ln2), __dmul_rn(__dmul_rn(2.0, s), acc));
 }
