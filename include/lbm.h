@@ -154,6 +154,48 @@ void lbm_destroy(lbm_t *h);
 
 const char *lbm_last_error(void);
 
+/* ---------------------------------------------------------------------------
+ * lbm_reduce_noalloc -- no counterpart in the reference.
+ *
+ * The sums of lbm_reduce (out[0] mass, out[1] kinetic energy, out[2] number
+ * of FLUID and MOVING sites) for a lattice state held in the caller's own
+ * device memory, computed without allocating anything.  It is meant for
+ * callers that cannot call cudaMalloc: code that runs while a CUDA graph is
+ * being captured (allocation cannot be captured), and processes whose device
+ * memory belongs to another allocator (a framework's caching pool, a fixed
+ * arena in a real-time loop) or is fully committed.  Such callers cannot
+ * create a handle (lbm_init allocates) but can pass pointers to buffers they
+ * own.
+ *
+ *   f      the populations in the LBM_DUMP_F_RAW layout of `precision`
+ *          (19 planes of dim^3 storage elements; the post-collision state
+ *          a handle holds after its last iteration)
+ *   map    the byte map (LBM_DUMP_MAP_U8), dim^3 bytes
+ *   lid    the lid u_x of each column, dim*dim values of the macro type
+ *          (double for LBM_FP64, float otherwise)
+ *   stream cudaStream_t to run on (NULL: the legacy default stream); the call
+ *          returns after the stream has finished the reduction
+ * All three buffers must be on the calling thread's current device.
+ *
+ * The block partial sums live in one fixed __device__ array of
+ * LBM_NOALLOC_SCRATCH_BYTES (32 KiB + 32 B) that every GPU which loads the
+ * library holds until the process exits; a launch uses at most
+ * LBM_NOALLOC_MAX_BLOCKS blocks per row kind so the partials always fit, and
+ * dim is limited to LBM_NOALLOC_MAX_DIM (larger: LBM_EINVAL).  The first call
+ * on a device looks up that array's device address (cudaGetSymbolAddress) with
+ * the device current; make that first call before any stream capture.  Every
+ * call reuses the same array, which keeps the last call's contents (the
+ * status word is cleared at the start of each call), so calls that overlap on
+ * the GPU -- on different streams, or from several host threads -- race and
+ * must be serialised by the caller.  Returns LBM_EDIVERGED (with out filled)
+ * when a density <= 0 or NaN was seen.
+ * ------------------------------------------------------------------------- */
+#define LBM_NOALLOC_MAX_BLOCKS 1024
+#define LBM_NOALLOC_MAX_DIM 2048
+#define LBM_NOALLOC_SCRATCH_BYTES ((4 * LBM_NOALLOC_MAX_BLOCKS + 4) * 8)
+int lbm_reduce_noalloc(const void *f, const uint8_t *map, const void *lid, int dim, int precision, void *stream,
+                       double out[3]);
+
 #ifdef __cplusplus
 }
 #endif

@@ -85,6 +85,8 @@ cudaError_t launch_sum_partials(const double *partials, int nblocks, double *out
     sum_partials_kernel<<<1, 256, 0, s>>>(partials, nblocks, out);
     return cudaGetLastError();
 }
+
+void set_last_error(const char *msg) { g_err = msg; }
 }  // namespace lbm
 
 struct lbm_handle {

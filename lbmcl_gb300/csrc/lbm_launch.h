@@ -30,4 +30,8 @@ LBM_DECLARE_LAUNCHERS(bf16)
 
 cudaError_t launch_sum_partials(const double *partials, int nblocks, double *out, cudaStream_t s);
 
+// Set the calling thread's lbm_last_error() text (for entry points defined
+// outside lbm_capi.cu).
+void set_last_error(const char *msg);
+
 }  // namespace lbm
