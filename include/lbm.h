@@ -140,6 +140,10 @@ int lbm_timing(lbm_t *h, double *total_ms, double *kernels_ms);
 /* Iterations run so far. */
 int lbm_iteration(const lbm_t *h, int64_t *it);
 
+/* Name of the CUDA device the handle runs on (replaces the CL_DEVICE_NAME
+ * query of lbmcl.hpp:626 and lbmcl.hpp:651). */
+const char *lbm_device_name(const lbm_t *h);
+
 /* The handle's CUDA stream (cudaStream_t), for callers that time or order
  * their own work against it. */
 void *lbm_stream(lbm_t *h);

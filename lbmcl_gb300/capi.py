@@ -87,6 +87,8 @@ def lib():
     L.lbm_destroy.argtypes = [vp]
     L.lbm_destroy.restype = None
     L.lbm_last_error.restype = C.c_char_p
+    L.lbm_device_name.argtypes = [vp]
+    L.lbm_device_name.restype = C.c_char_p
     for name in ("lbm_init", "lbm_step", "lbm_dump", "lbm_load", "lbm_sync", "lbm_timing", "lbm_iteration",
                  "lbm_reduce"):
         getattr(L, name).restype = C.c_int
@@ -183,6 +185,10 @@ class Lattice:
         tot, ker = C.c_double(), C.c_double()
         check(lib().lbm_timing(self.h, C.byref(tot), C.byref(ker)))
         return tot.value, ker.value
+
+    @property
+    def device_name(self) -> str:
+        return lib().lbm_device_name(self.h).decode()
 
     def reduce(self):
         out = (C.c_double * 3)()

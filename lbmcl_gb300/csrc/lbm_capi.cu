@@ -122,6 +122,7 @@ struct lbm_handle {
     int rows = 1, gpp = 0, stages = 0;
     unsigned ngroups = 0, sgrid = 0, sblock = 0;
     size_t ssmem = 0;
+    std::string device_name;
 };
 
 namespace {
@@ -391,6 +392,9 @@ int lbm_init(lbm_t **out, const lbm_config *c)
     int rc = LBM_OK;
     auto setup = [&]() -> int {
         LBM_CUDA(cudaSetDevice(c->device));
+        cudaDeviceProp prop;
+        LBM_CUDA(cudaGetDeviceProperties(&prop, c->device));
+        h->device_name = prop.name;
         LBM_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
         LBM_CUDA(cudaEventCreate(&h->ev_first));
         LBM_CUDA(cudaEventCreate(&h->ev_last));
@@ -631,6 +635,8 @@ int lbm_iteration(const lbm_t *h, int64_t *it)
 }
 
 void *lbm_stream(lbm_t *h) { return h ? (void *)h->stream : nullptr; }
+
+const char *lbm_device_name(const lbm_t *h) { return h ? h->device_name.c_str() : ""; }
 
 int lbm_reduce(lbm_t *h, double out[3])
 {

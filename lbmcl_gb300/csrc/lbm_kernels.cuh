@@ -361,6 +361,47 @@ __device__ __forceinline__ void accumulate(const SiteOut &o, double &m, double &
     e += 0.5 * o.r * (o.ux * o.ux + o.uy * o.uy + o.uz * o.uz);
 }
 
+// Any mix of site kinds (face rows): per-site, map-driven update.
+template <class S, int MODE, int V>
+__device__ __forceinline__ void update_general(S (&fs)[Q][V], typename MapWord<V>::type mw, const StepArgs &a,
+                                               int y, int z, int x0, size_t site0, double &red_m, double &red_e)
+{
+    using C = typename Compute<S>::type;
+    constexpr bool DEV = is_dev16<S>();
+    const int dim = a.dim;
+    const bool lid_row = (z == dim - 2);
+    const C *lid = static_cast<const C *>(a.lid);
+    const Weights<C> W = make_weights<C>();
+    const C inv_tau = (C)a.inv_tau;
+    const DevK K = make_devk(a.omega_f, Dev16<S>::scale, Dev16<S>::inv_scale);
+    bool bad = false;
+#pragma unroll
+    for (int k = 0; k < V; ++k) {
+        const uint8_t b = (uint8_t)(mw >> (8 * k));
+        const C lidv = lid_row ? lid[(size_t)y * dim + x0 + k] : (C)0;
+        SiteOut o;
+        if constexpr (DEV) {
+            float D[Q];
+#pragma unroll
+            for (int i = 0; i < Q; ++i) D[i] = Dev16<S>::to_f(fs[i][k]);
+            site_dev<MODE != MODE_REDUCE>(D, b, (float)lidv, K, Dev16<S>::scale, o);
+#pragma unroll
+            for (int i = 0; i < Q; ++i) fs[i][k] = Dev16<S>::from_f(D[i]);
+        } else {
+            C f[Q];
+#pragma unroll
+            for (int i = 0; i < Q; ++i) f[i] = fs[i][k];
+            site_exact<C, MODE != MODE_REDUCE>(f, b, lidv, inv_tau, W, o);
+#pragma unroll
+            for (int i = 0; i < Q; ++i) fs[i][k] = f[i];
+        }
+        bad |= o.bad;
+        if (MODE == MODE_STEP_MACRO && o.macro) store_macro<C>(a, site0 + k, o);
+        if (MODE == MODE_REDUCE && o.macro) accumulate(o, red_m, red_e);
+    }
+    if (bad) atomicOr(a.status, 1);
+}
+
 // Update the V sites x0..x0+V-1 of row (y, z) in place: fs holds their pulled
 // populations on entry and their post-collision populations on exit.  Stores
 // rho / u (MODE_STEP_MACRO) or accumulates the reduction sums (MODE_REDUCE).
@@ -371,8 +412,6 @@ __device__ __forceinline__ void update_vector(S (&fs)[Q][V], typename MapWord<V>
     using C = typename Compute<S>::type;
     constexpr bool DEV = is_dev16<S>();
     const int dim = a.dim;
-    const bool lid_row = (z == dim - 2);
-    const C *lid = static_cast<const C *>(a.lid);
     const Weights<C> W = make_weights<C>();
     const C inv_tau = (C)a.inv_tau;
     bool bad = false;
@@ -436,33 +475,9 @@ __device__ __forceinline__ void update_vector(S (&fs)[Q][V], typename MapWord<V>
             return;
         }
     }
-
-#pragma unroll
-    for (int k = 0; k < V; ++k) {
-        const uint8_t b = (uint8_t)(mw >> (8 * k));
-        const C lidv = lid_row ? lid[(size_t)y * dim + x0 + k] : (C)0;
-        SiteOut o;
-        if constexpr (DEV) {
-            float D[Q];
-#pragma unroll
-            for (int i = 0; i < Q; ++i) D[i] = Dev16<S>::to_f(fs[i][k]);
-            site_dev<MODE != MODE_REDUCE>(D, b, (float)lidv, K, Dev16<S>::scale, o);
-#pragma unroll
-            for (int i = 0; i < Q; ++i) fs[i][k] = Dev16<S>::from_f(D[i]);
-        } else {
-            C f[Q];
-#pragma unroll
-            for (int i = 0; i < Q; ++i) f[i] = fs[i][k];
-            site_exact<C, MODE != MODE_REDUCE>(f, b, lidv, inv_tau, W, o);
-#pragma unroll
-            for (int i = 0; i < Q; ++i) fs[i][k] = f[i];
-        }
-        bad |= o.bad;
-        if (MODE == MODE_STEP_MACRO && o.macro) store_macro<C>(a, site0 + k, o);
-        if (MODE == MODE_REDUCE && o.macro) accumulate(o, red_m, red_e);
-    }
-    if (bad) atomicOr(a.status, 1);
+    if constexpr (!FLUID_ONLY) update_general<S, MODE, V>(fs, mw, a, y, z, x0, site0, red_m, red_e);
 }
+
 
 // Bounce-back of the x-face site x = xf of an interior row (y, z in
 // [2, dim-3]): its output population i is its pulled input of the opposite

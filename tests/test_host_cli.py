@@ -1,0 +1,158 @@
+"""The lbmcl host program (C++ over the C ABI): the reference's command line,
+its output files byte for byte, and make test8 / make test32 against the
+reference's golden data."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+@pytest.fixture(scope="module")
+def lbmcl_bin():
+    from lbmcl_gb300 import build
+    build.build_library()
+    return build.build_host()
+
+
+def run(binary, *args, cwd=None):
+    return subprocess.run([binary, *map(str, args)], capture_output=True, text=True, cwd=cwd, timeout=600)
+
+
+# ---------------------------------------------------------------- CPU ------
+def test_help_and_exit_code(lbmcl_bin):
+    r = run(lbmcl_bin, "-h")
+    assert r.returncode == 1  # lbm_options.hpp:103-122 exits 1
+    for flag in ("-d  --dim", "-n  --viscosity", "-u  --velocity", "-i  --iterations", "-e  --every",
+                 "-F  --use_double", "-s  --stride", "--precision"):
+        assert flag in r.stdout
+
+
+@pytest.mark.parametrize("args,msg", [
+    (["-d", "-3"], "Please enter a valid lattice dimension"),
+    (["-i", "-1"], "Please enter a valid number of iterations"),
+    (["-n", "-0.1"], "Please enter a valid viscosity value"),
+    (["-e", "-2"], "Please enter a valid number for save simulation results every N iterations"),
+    (["-s", "-4"], "Please enter a valid number for stride value"),
+    (["--precision", "fp8"], "Please enter a valid precision"),
+])
+def test_rejects_bad_values(lbmcl_bin, args, msg):
+    r = run(lbmcl_bin, *args)
+    assert r.returncode == 1 and msg in r.stderr
+
+
+def test_rounds_dim_and_stride_like_the_reference(lbmcl_bin, tmp_path):
+    # the messages come from the constructor, before any device work
+    r = run(lbmcl_bin, "-d", "12", "-s", "24", "-i", "0", "-e", "0", "-v", tmp_path)
+    assert "dim is rounded to the previous power of 2: 8" in r.stdout
+    assert "stride is rounded to the previous power of 2: 16" in r.stdout
+
+
+def test_rejects_oversized_work_group(lbmcl_bin):
+    r = run(lbmcl_bin, "-d", "4", "-w", "8,8,8")
+    assert r.returncode == 255 and "Please enter a good work_group_size" in r.stderr
+
+
+# -------------------------------------------------------- renderers ------
+def render_f_dump(f, dim, stride):
+    """lbmcl.hpp:206-258 for one CSoA buffer."""
+    dd = len(str(dim)) if dim > 0 else 1
+    head = " " * (dd * 3 + 5) + "".join("%8d " % q for q in range(19)) + "\n"
+    out = []
+    for z in range(dim):
+        for y in range(dim):
+            out.append(head)
+            for x in range(dim):
+                i = x + y * dim + z * dim * dim
+                vals = "".join("%8.6f " % float(f[((i // stride) * 19 + q) * stride + (i & (stride - 1))])
+                               for q in range(19))
+                out.append(("(".rjust(dd)) + "%d,%d,%d) " % (x, y, z) + vals + "\n")
+            out.append("\n")
+        out.append("\n")
+    out.append("\n")
+    return "".join(out)
+
+
+def render_map(cmap, dim):
+    """lbmcl.hpp:159-203."""
+    def code(c):
+        v = 0
+        if c == 0x1: v = 1
+        if c & 0x2: v = 2
+        if c & 0x3F0: v = 3
+        if c == 0x8: v = 4
+        if c == 0x4: v = 5
+        return v
+    out = ["# FLUID       1\n# MOVING      2\n# BOUNDARY    3\n# WALL        4\n# CORNER      5\n\n"]
+    for z in range(dim):
+        for y in range(dim):
+            out.append("".join("%d " % code(cmap[x + y * dim + z * dim * dim]) for x in range(dim)) + "\n")
+        out.append("\n")
+    out.append("\n")
+    return "".join(out)
+
+
+# ---------------------------------------------------------------- GPU ------
+@pytest.mark.gpu
+def test_make_test8_files_byte_identical(lbmcl_bin, oracle, tmp_path, capi):
+    """make testall at 8^3 (-f -m, every iteration): f_<it>.dump, map.dump and
+    lbmcl.<it>.vti equal the reference's files for the same run (rendered
+    from the oracle, which is bit-identical to the reference kernel)."""
+    from lbmcl_gb300 import vti
+    r = run(lbmcl_bin, "-d", 8, "-n", 0.0089, "-u", 0.05, "-i", 10, "-e", 1, "-w", "8,8,8", "-s", 8,
+            "-v", tmp_path, "-p", tmp_path, "-f", "-m")
+    assert r.returncode == 0, r.stderr
+    o = oracle.OracleLattice(8, 0.0089, 0.05, "f32", 8)
+    assert (tmp_path / "map.dump").read_text() == render_map(o.map, 8)
+    ref_vti = tmp_path / "ref.vti"
+    vti.write_vti_ascii(str(ref_vti), 8, o.rho, o.u)
+    assert (tmp_path / "lbmcl.00.vti").read_text() == ref_vti.read_text()
+    assert (tmp_path / "f_00.dump").read_text() == render_f_dump(o.state, 8, 8)
+    for it in range(1, 11):
+        # f_<it> is the buffer iteration it reads (lbmcl.hpp:517-519)
+        assert (tmp_path / f"f_{it:02d}.dump").read_text() == render_f_dump(o.state, 8, 8), it
+        o.step(1, every=1)
+        vti.write_vti_ascii(str(ref_vti), 8, o.rho, o.u)
+        assert (tmp_path / f"lbmcl.{it:02d}.vti").read_text() == ref_vti.read_text(), it
+    g8 = np.load(os.path.join(GOLD, "sailfish_ldc8.npz"))
+    for it in range(0, 11):
+        got = vti.read_vti(str(tmp_path / f"lbmcl.{it:02d}.vti"))
+        c = vti.compare({"rho": g8[f"rho_{it}"], "v": g8[f"v_{it}"]}, got)
+        assert c["mae_rho"] < 2e-6 and c["mae_v"] < 1e-6, (it, c)
+    assert "Kernels MLUPS:" in r.stdout and r.stderr.count(";") == 11
+
+
+@pytest.mark.gpu
+def test_make_test32_against_golden(lbmcl_bin, tmp_path, capi):
+    """make test32 (Makefile:81-86): 500 iterations, every 20, -w 32,32,1 -s 32."""
+    from lbmcl_gb300 import vti
+    r = run(lbmcl_bin, "-d", 32, "-n", 0.0089, "-u", 0.05, "-i", 500, "-e", 20, "-w", "32,32,1", "-s", 32,
+            "-v", tmp_path)
+    assert r.returncode == 0, r.stderr
+    assert len(list(tmp_path.glob("lbmcl.*.vti"))) == 26
+    g = np.load(os.path.join(GOLD, "sailfish_ldc32.npz"))
+    for it in (20, 500):
+        got = vti.read_vti(str(tmp_path / f"lbmcl.{it:03d}.vti"))
+        c = vti.compare({"rho": g[f"rho_{it}"], "v": g[f"v_{it}"]}, got)
+        assert c["mae_rho"] < 5e-6 and c["mae_v"] < 2e-6, (it, c)
+
+
+@pytest.mark.gpu
+def test_double_and_sixteen_bit_runs(lbmcl_bin, oracle, tmp_path, capi):
+    from lbmcl_gb300 import vti
+    r = run(lbmcl_bin, "-d", 16, "-i", 7, "-e", 7, "-F", "-s", 16, "-v", tmp_path)
+    assert r.returncode == 0, r.stderr
+    o = oracle.OracleLattice(16, 0.0089, 0.05, "f64", 16)
+    o.step(7, every=7)
+    ref_vti = tmp_path / "ref.vti"
+    vti.write_vti_ascii(str(ref_vti), 16, o.rho, o.u)
+    assert (tmp_path / "lbmcl.7.vti").read_text() == ref_vti.read_text()
+    for p in ("fp16", "bf16"):
+        d = tmp_path / p
+        d.mkdir()
+        r = run(lbmcl_bin, "-d", 32, "-i", 40, "-e", 40, "--precision", p, "--seed", 5, "--noise", 1e-4, "-v", d)
+        assert r.returncode == 0, r.stderr
+        got = vti.read_vti(str(d / "lbmcl.40.vti"))
+        assert np.isfinite(np.nan_to_num(got["rho"], nan=1.0)).all()
