@@ -875,12 +875,12 @@ __global__ void init_kernel(InitArgs a)
                         d = deq_scaled(i, 0.0f, 1.0f, eu, 1.5f * (float)lv * (float)lv, 1.0f);
                     }
                     if (a.noise_sigma != 0.0 && tb == 0)
-                        d = d + (float)__dmul_rn(a.noise_sigma, gauss(a.seed, tid, (uint32_t)i));
+                        d = d + (float)__dmul_rn(a.noise_sigma, (double)gauss(a.seed, tid, (uint32_t)i));
                     val = d * Dev16<S>::scale;
                 } else {
                     val = (tb & M_FRONT) ? init_eq_exact<C>(i, lv, W) : W.w[wclass_of(i)];
                     if (a.noise_sigma != 0.0 && tb == 0)
-                        val = X<C>::add(val, (C)__dmul_rn(a.noise_sigma, gauss(a.seed, tid, (uint32_t)i)));
+                        val = X<C>::add(val, (C)__dmul_rn(a.noise_sigma, (double)gauss(a.seed, tid, (uint32_t)i)));
                 }
             }
         }

@@ -1,11 +1,13 @@
 // lbm_noise.cuh -- seeded Gaussian perturbation of the initial populations.
 //
 // N(0,1) sample for (seed, site, q): Philox4x32-10 (Salmon, Moraes, Dror,
-// Shaw, SC'11) on the counter (site_lo, site_hi, q, attempt), two 53-bit
-// uniforms per block, Marsaglia's polar method, and a natural logarithm
+// Shaw, SC'11) on the counter (site_lo, site_hi, q, block), two 24-bit
+// uniform pairs per block, Marsaglia's polar method, and a natural logarithm
 // summed from the atanh series.  Every floating-point step is an explicit
-// IEEE double operation (no contraction, no library transcendental), so a
-// CPU implementation of the same recipe gets the same bits.
+// IEEE single-precision operation (no contraction, no library
+// transcendental), so a CPU implementation of the same recipe gets the same
+// bits.  Single precision because FP64 runs at a small fraction of the FP32
+// rate on GB300 and the samples only perturb the initial state.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -32,58 +34,60 @@ __device__ __forceinline__ void philox4x32_10(uint32_t c[4], uint32_t k0, uint32
     }
 }
 
-// ln(x), x finite and > 0: x = m 2^e, m in [sqrt(1/2), sqrt(2)),
-// ln m = 2 s sum_{k=0..11} s^(2k) / (2k+1), s = (m-1)/(m+1).
-__device__ __forceinline__ double series_log(double x)
+// ln(x), x finite and > 0, single precision: x = m 2^e, m in
+// [sqrt(1/2), sqrt(2)), ln m = 2 s sum_{k=0..6} s^(2k) / (2k+1), s = (m-1)/(m+1).
+__device__ __forceinline__ float series_logf(float x)
 {
-    long long bits = __double_as_longlong(x);
-    int e = (int)((bits >> 52) & 0x7ff);
+    unsigned bits = __float_as_uint(x);
+    int e = (int)((bits >> 23) & 0xff);
     if (e == 0) {
-        x = __dmul_rn(x, 18014398509481984.0);  // 2^54, exact
-        bits = __double_as_longlong(x);
-        e = (int)((bits >> 52) & 0x7ff) - 54;
+        x = __fmul_rn(x, 16777216.0f);  // 2^24, exact
+        bits = __float_as_uint(x);
+        e = (int)((bits >> 23) & 0xff) - 24;
     }
-    e -= 1023;
-    bits = (bits & 0x000fffffffffffffll) | 0x3ff0000000000000ll;
-    double m = __longlong_as_double(bits);
-    if (m > 1.4142135623730951) {
-        m = __dmul_rn(m, 0.5);
+    e -= 127;
+    bits = (bits & 0x007fffffu) | 0x3f800000u;
+    float m = __uint_as_float(bits);
+    if (m > 1.41421354f) {
+        m = __fmul_rn(m, 0.5f);
         e += 1;
     }
-    const double s = __ddiv_rn(__dsub_rn(m, 1.0), __dadd_rn(m, 1.0));
-    const double s2 = __dmul_rn(s, s);
-    // 1 / (2k + 1), k = 0 .. 11, folded at compile time to the correctly
-    // rounded doubles (the values an IEEE division yields at run time)
-    constexpr double inv_odd[12] = {1.0 / 1.0,  1.0 / 3.0,  1.0 / 5.0,  1.0 / 7.0,  1.0 / 9.0,  1.0 / 11.0,
-                                    1.0 / 13.0, 1.0 / 15.0, 1.0 / 17.0, 1.0 / 19.0, 1.0 / 21.0, 1.0 / 23.0};
-    double acc = inv_odd[11];
+    const float s = __fdiv_rn(__fsub_rn(m, 1.0f), __fadd_rn(m, 1.0f));
+    const float s2 = __fmul_rn(s, s);
+    // 1 / (2k + 1), folded at compile time to the correctly rounded floats
+    constexpr float inv_odd[7] = {1.0f / 1.0f, 1.0f / 3.0f, 1.0f / 5.0f,  1.0f / 7.0f,
+                                  1.0f / 9.0f, 1.0f / 11.0f, 1.0f / 13.0f};
+    float acc = inv_odd[6];
 #pragma unroll
-    for (int k = 10; k >= 0; --k) acc = __dadd_rn(inv_odd[k], __dmul_rn(s2, acc));
-    const double ln2 = 0.6931471805599453;
-    return __dadd_rn(__dmul_rn((double)e, ln2), __dmul_rn(__dmul_rn(2.0, s), acc));
+    for (int k = 5; k >= 0; --k) acc = __fadd_rn(inv_odd[k], __fmul_rn(s2, acc));
+    const float ln2 = 0.693147182f;
+    return __fadd_rn(__fmul_rn((float)e, ln2), __fmul_rn(__fmul_rn(2.0f, s), acc));
 }
 
-__device__ __forceinline__ double sym_uniform(uint32_t a, uint32_t b)
+__device__ __forceinline__ float sym_uniform(uint32_t a)
 {
-    const unsigned long long m = ((unsigned long long)(a >> 5) << 26) | (unsigned long long)(b >> 6);
-    const double u01 = __dmul_rn(__dadd_rn((double)m, 0.5), 1.0 / 9007199254740992.0);
-    return __dsub_rn(__dmul_rn(2.0, u01), 1.0);
+    const float u01 = __fmul_rn(__fadd_rn((float)(a >> 8), 0.5f), 1.0f / 16777216.0f);
+    return __fsub_rn(__fmul_rn(2.0f, u01), 1.0f);
 }
 
-__device__ __forceinline__ double gauss(uint64_t seed, uint64_t site, uint32_t q)
+// Marsaglia polar method; each Philox block gives two attempts (32 blocks at most).
+__device__ __forceinline__ float gauss(uint64_t seed, uint64_t site, uint32_t q)
 {
     const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
-    for (uint32_t attempt = 0; attempt < 64; ++attempt) {
-        uint32_t c[4] = {(uint32_t)site, (uint32_t)(site >> 32), q, attempt};
+    for (uint32_t block = 0; block < 32; ++block) {
+        uint32_t c[4] = {(uint32_t)site, (uint32_t)(site >> 32), q, block};
         philox4x32_10(c, k0, k1);
-        const double v1 = sym_uniform(c[0], c[1]);
-        const double v2 = sym_uniform(c[2], c[3]);
-        const double s = __dadd_rn(__dmul_rn(v1, v1), __dmul_rn(v2, v2));
-        if (s >= 1.0 || s == 0.0) continue;
-        const double t = __ddiv_rn(__dmul_rn(-2.0, series_log(s)), s);
-        return __dmul_rn(v1, __dsqrt_rn(t));
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+            const float v1 = sym_uniform(c[2 * half]);
+            const float v2 = sym_uniform(c[2 * half + 1]);
+            const float s = __fadd_rn(__fmul_rn(v1, v1), __fmul_rn(v2, v2));
+            if (s >= 1.0f || s == 0.0f) continue;
+            const float t = __fdiv_rn(__fmul_rn(-2.0f, series_logf(s)), s);
+            return __fmul_rn(v1, __fsqrt_rn(t));
+        }
     }
-    return 0.0;
+    return 0.0f;
 }
 
 }  // namespace lbm

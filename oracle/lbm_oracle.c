@@ -97,60 +97,67 @@ void lbmo_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t o
     out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
 }
 
-/* ln(x) for finite x > 0: x = m 2^e with m in [sqrt(1/2), sqrt(2)), then
- * ln m = 2 atanh(s), s = (m-1)/(m+1), summed as the odd series
- * 2 s (1 + s^2/3 + s^4/5 + ... + s^22/23) (|s| <= 0.1716, so the truncation
- * error is below 1e-18).  Uses only IEEE + - * /, no library call. */
-double lbmo_log(double x)
+/* ln(x) for finite x > 0 in single precision: x = m 2^e with m in
+ * [sqrt(1/2), sqrt(2)), ln m = 2 atanh(s), s = (m-1)/(m+1), summed as the odd
+ * series 2 s (1 + s^2/3 + ... + s^12/13) (|s| <= 0.1716: truncation below
+ * 1e-9).  IEEE float + - * / only, no library call. */
+float lbmo_logf(float x)
 {
-    uint64_t bits;
+    uint32_t bits;
     memcpy(&bits, &x, sizeof bits);
-    int e = (int)((bits >> 52) & 0x7ff);
-    if (e == 0) { /* subnormal: scale by 2^54 exactly */
-        x = x * 18014398509481984.0;
+    int e = (int)((bits >> 23) & 0xff);
+    if (e == 0) { /* subnormal: scale by 2^24 exactly */
+        x = x * 16777216.0f;
         memcpy(&bits, &x, sizeof bits);
-        e = (int)((bits >> 52) & 0x7ff) - 54;
+        e = (int)((bits >> 23) & 0xff) - 24;
     }
-    e -= 1023;
-    bits = (bits & 0x000fffffffffffffull) | 0x3ff0000000000000ull; /* m in [1,2) */
-    double m;
+    e -= 127;
+    bits = (bits & 0x007fffffu) | 0x3f800000u; /* m in [1,2) */
+    float m;
     memcpy(&m, &bits, sizeof m);
-    if (m > 1.4142135623730951) { m = m * 0.5; e += 1; }
-    const double s = (m - 1.0) / (m + 1.0);
-    const double s2 = s * s;
-    double acc = 1.0 / 23.0;
-    for (int k = 10; k >= 0; --k) acc = (1.0 / (double)(2 * k + 1)) + s2 * acc;
-    /* the loop above starts at 1/23 and folds 1/21 .. 1/1 in: acc = sum s2^k/(2k+1) */
-    const double ln2 = 0.6931471805599453;
-    return ((double)e * ln2) + ((2.0 * s) * acc);
+    if (m > 1.41421354f) { m = m * 0.5f; e += 1; }
+    const float s = (m - 1.0f) / (m + 1.0f);
+    const float s2 = s * s;
+    static const float inv_odd[7] = {1.0f / 1.0f, 1.0f / 3.0f, 1.0f / 5.0f, 1.0f / 7.0f,
+                                     1.0f / 9.0f, 1.0f / 11.0f, 1.0f / 13.0f};
+    float acc = inv_odd[6];
+    for (int k = 5; k >= 0; --k) acc = inv_odd[k] + s2 * acc;
+    const float ln2 = 0.693147182f;
+    return ((float)e * ln2) + ((2.0f * s) * acc);
 }
 
-/* Uniform in (-1, 1) from two 32-bit words (53 random bits). */
-static inline double lbmo_sym_uniform(uint32_t a, uint32_t b)
+double lbmo_log(double x) { return (double)lbmo_logf((float)x); }
+
+/* Uniform in (-1, 1) from a 32-bit word (24 random bits). */
+static inline float lbmo_sym_uniform(uint32_t a)
 {
-    const uint64_t m = ((uint64_t)(a >> 5) << 26) | (uint64_t)(b >> 6);
-    const double u01 = ((double)m + 0.5) * (1.0 / 9007199254740992.0);
-    return (2.0 * u01) - 1.0;
+    const float u01 = ((float)(a >> 8) + 0.5f) * (1.0f / 16777216.0f);
+    return (2.0f * u01) - 1.0f;
 }
 
 /* Standard normal by the Marsaglia polar method on the counter stream
- * (site, q, attempt); attempt is bounded, so the loop always ends. */
-double lbmo_gauss(uint64_t seed, uint64_t site, uint32_t q)
+ * (site, q, attempt), single precision; each Philox block offers two
+ * attempts; at most 64 attempts, so the loop always ends. */
+float lbmo_gaussf(uint64_t seed, uint64_t site, uint32_t q)
 {
     const uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
-    for (uint32_t attempt = 0; attempt < 64; ++attempt) {
-        const uint32_t ctr[4] = {(uint32_t)site, (uint32_t)(site >> 32), q, attempt};
+    for (uint32_t block = 0; block < 32; ++block) {
+        const uint32_t ctr[4] = {(uint32_t)site, (uint32_t)(site >> 32), q, block};
         uint32_t r[4];
         lbmo_philox4x32_10(ctr, key, r);
-        const double v1 = lbmo_sym_uniform(r[0], r[1]);
-        const double v2 = lbmo_sym_uniform(r[2], r[3]);
-        const double s = (v1 * v1) + (v2 * v2);
-        if (s >= 1.0 || s == 0.0) continue;
-        const double t = (-2.0 * lbmo_log(s)) / s;
-        return v1 * sqrt(t);
+        for (int half = 0; half < 2; ++half) {
+            const float v1 = lbmo_sym_uniform(r[2 * half]);
+            const float v2 = lbmo_sym_uniform(r[2 * half + 1]);
+            const float s = (v1 * v1) + (v2 * v2);
+            if (s >= 1.0f || s == 0.0f) continue;
+            const float t = (-2.0f * lbmo_logf(s)) / s;
+            return v1 * sqrtf(t);
+        }
     }
-    return 0.0;
+    return 0.0f;
 }
+
+double lbmo_gauss(uint64_t seed, uint64_t site, uint32_t q) { return (double)lbmo_gaussf(seed, site, q); }
 
 /* ---- precision-generic body, instantiated for float and double ---------- */
 #define REAL float

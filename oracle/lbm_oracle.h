@@ -62,13 +62,16 @@ int lbmo_cell_type(int dim, int x, int y, int z);
 
 /* Standard normal sample for (seed, site, q): Philox4x32-10 counter stream,
  * Marsaglia polar method, a self-contained natural logarithm.  Computed with
- * IEEE double + - * / sqrt only, so the GPU library reproduces it bit for bit. */
+ * IEEE single-precision + - * / sqrt only, so the GPU library reproduces it
+ * bit for bit.  lbmo_gauss returns the same value widened to double. */
+float lbmo_gaussf(uint64_t seed, uint64_t site, uint32_t q);
 double lbmo_gauss(uint64_t seed, uint64_t site, uint32_t q);
 
 /* Philox4x32-10 block (Salmon et al., SC'11), exposed for known-answer tests. */
 void lbmo_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 
-/* Natural logarithm used by lbmo_gauss (x > 0, finite). */
+/* Natural logarithm used by lbmo_gaussf (x > 0, finite); lbmo_log widens it. */
+float lbmo_logf(float x);
 double lbmo_log(double x);
 
 /* initialize (kernels.cl:277-318), then noise on FLUID sites of both buffers. */
