@@ -154,6 +154,38 @@ void *lbm_stream(lbm_t *h);
  * such sites.  Moments as kernels.cl:352-380 defines them.  Synchronous. */
 int lbm_reduce(lbm_t *h, double out[3]);
 
+/* ---------------------------------------------------------------------------
+ * Gradients (new; the reference has no adjoint).
+ *
+ * Loss: J = mean over the FLUID sites of the plane y = plane_y of
+ * (u_x - target(x, z))^2, u_x the velocity of the buffer the next iteration
+ * would read (the post-stream state R_T after T iterations).  Controls: the
+ * per-column lid velocity, tau, and the initial populations R_0 (the state
+ * the adjoint forward starts from, in the LBM_DUMP_F layout).
+ * ------------------------------------------------------------------------- */
+
+/* Set the loss plane (2 <= plane_y <= dim-3) and the u_x target,
+ * target_ux[x + z*dim] (NULL: zero). */
+int lbm_adjoint_set_loss(lbm_t *h, int plane_y, const double *target_ux);
+
+/* Run `iterations` iterations from the current state (as lbm_step without
+ * macro output), keeping a checkpoint of the state every `checkpoint_every`
+ * iterations (1 = the whole trajectory), and return the loss of the final
+ * state.  Synchronous. */
+int lbm_adjoint_forward(lbm_t *h, int iterations, int checkpoint_every, double *loss);
+
+/* Backward sweep of the last lbm_adjoint_forward, scaled by dloss (dL/dJ for
+ * a caller's outer loss L): hand-written adjoint kernels, each checkpoint
+ * segment recomputed with the forward kernel.  Any output may be NULL:
+ *   grad_tau   dL/dtau
+ *   grad_lid   dim*dim doubles, dL/dlid at [x + y*dim]
+ *   grad_f0    dL/dR_0 in the LBM_DUMP_F layout and type (grad_f0_bytes =
+ *              lbm_size(h, LBM_DUMP_F)); when R_0 is the state lbm_init made,
+ *              its dependence on the lid is included in grad_lid.
+ * Adjoint arithmetic: FP64 for an FP64 handle, FP32 otherwise.  Synchronous. */
+int lbm_adjoint_backward(lbm_t *h, double dloss, double *grad_tau, double *grad_lid, void *grad_f0,
+                         size_t grad_f0_bytes);
+
 void lbm_destroy(lbm_t *h);
 
 const char *lbm_last_error(void);

@@ -89,8 +89,11 @@ def lib():
     L.lbm_last_error.restype = C.c_char_p
     L.lbm_device_name.argtypes = [vp]
     L.lbm_device_name.restype = C.c_char_p
+    L.lbm_adjoint_set_loss.argtypes = [vp, C.c_int, C.POINTER(C.c_double)]
+    L.lbm_adjoint_forward.argtypes = [vp, C.c_int, C.c_int, C.POINTER(C.c_double)]
+    L.lbm_adjoint_backward.argtypes = [vp, C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_double), vp, sz]
     for name in ("lbm_init", "lbm_step", "lbm_dump", "lbm_load", "lbm_sync", "lbm_timing", "lbm_iteration",
-                 "lbm_reduce"):
+                 "lbm_reduce", "lbm_adjoint_set_loss", "lbm_adjoint_forward", "lbm_adjoint_backward"):
         getattr(L, name).restype = C.c_int
     _lib = L
     return L
@@ -229,6 +232,33 @@ class Lattice:
     def load_f(self, f: np.ndarray):
         f = np.ascontiguousarray(f, self.fdtype)
         check(lib().lbm_load(self.h, DUMP_F, f.ctypes.data_as(C.c_void_p), f.nbytes))
+
+    # -- gradients -------------------------------------------------------------
+    def adjoint_set_loss(self, plane_y: int, target_ux=None):
+        """Loss = mean over the FLUID sites of plane y of (u_x - target)^2;
+        target_ux indexed [z, x] (or flat x + z*dim), None = 0."""
+        t = None
+        if target_ux is not None:
+            self._target = np.ascontiguousarray(np.asarray(target_ux, np.float64).reshape(-1))
+            assert self._target.size == self.dim * self.dim
+            t = self._target.ctypes.data_as(C.POINTER(C.c_double))
+        check(lib().lbm_adjoint_set_loss(self.h, int(plane_y), t))
+
+    def adjoint_forward(self, iterations: int, checkpoint_every: int) -> float:
+        loss = C.c_double()
+        check(lib().lbm_adjoint_forward(self.h, int(iterations), int(checkpoint_every), C.byref(loss)))
+        return loss.value
+
+    def adjoint_backward(self, dloss: float = 1.0, want_f0: bool = True):
+        """Returns (dL/dtau, dL/dlid as [y, x], dL/dR_0 in the F layout or None)."""
+        gt = C.c_double()
+        glid = np.zeros(self.dim * self.dim, np.float64)
+        gf0 = np.empty(self.size(DUMP_F) // np.dtype(self.fdtype).itemsize, self.fdtype) if want_f0 else None
+        check(lib().lbm_adjoint_backward(self.h, float(dloss), C.byref(gt),
+                                         glid.ctypes.data_as(C.POINTER(C.c_double)),
+                                         gf0.ctypes.data_as(C.c_void_p) if gf0 is not None else None,
+                                         gf0.nbytes if gf0 is not None else 0))
+        return gt.value, glid.reshape(self.dim, self.dim), gf0
 
     def load_raw(self, raw: np.ndarray):
         raw = np.ascontiguousarray(raw)

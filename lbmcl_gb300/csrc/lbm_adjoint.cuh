@@ -1,0 +1,314 @@
+// lbm_adjoint.cuh -- hand-written adjoint of the D3Q19 BGK cavity iteration.
+//
+// Written in the reference's post-stream form.  With R_k the buffer iteration
+// k+1 reads (kernels.cl:339-341) and C the local collision with its boundary
+// rules (kernels.cl:343-418),
+//     R_{k+1} = S C(R_k),   S: slot (s, i) <- site s - e_i, slot i.
+// For a loss J(R_T), the adjoint a_k = dJ/dR_k obeys
+//     a_k(s, .) = J_C(R_k(s))^T b(s),   b_i(s) = a_{k+1}(s + e_i, i),
+// i.e. "pull from s + e_i (reverse streaming), then apply the transposed
+// local Jacobian" -- the same data movement as the forward step with the
+// shifts reversed.  Walls never compute and their adjoint stays 0, which makes
+// b_i = 0 wherever the forward pushed into a wall.  Slots whose forward source
+// is a wall hold constants; their adjoint is never pulled again.
+//
+// Transposed Jacobians of C at a site with pre-collision g (R_k(s)):
+//  FLUID   (BGK, omega = 1/tau): with rho, u of g, p_i = 1 + 3 e.u + 4.5 (e.u)^2
+//          - 1.5 u^2, feq_i = w_i rho p_i,
+//            B0 = sum_i b_i w_i p_i,
+//            G  = sum_i b_i w_i (3 + 9 e_i.u) e_i - 3 u sum_i b_i w_i,
+//            a_j = (1 - omega) b_j + omega (B0 - G.u + G.e_j),
+//          and dJ/domega += sum_i b_i (feq_i - g_i).
+//  MOVING  (lid, kernels.cl:343-349, 393-398): out_i = w_i rho p_i(lid) with
+//          rho over g after the -z replacements, so
+//            a_j = m_j sum_i b_i w_i p_i,  m_j = 0 for j in {5,11,12,13,14},
+//            2 for j in {6,15,16,17,18}, 1 otherwise,
+//          and dJ/dlid(x,y) += sum_i b_i w_i rho (3 e_ix + (9 e_ix^2 - 3) lid).
+//  bounce-back: a_j = b_opp(j);  CORNER: a_j = b_j;  WALL: a = 0.
+#pragma once
+
+#include "lbm_kernels.cuh"
+
+namespace lbm {
+
+struct AdjArgs {
+    const void *fwd;     // forward state Q_k (the P buffer iteration k+1 reads from)
+    const void *ain;     // a_{k+1}, adjoint type, post-stream layout [q][z][y][x]
+    void *aout;          // a_k
+    const uint8_t *map;
+    const void *lid;     // forward macro type, dim*dim
+    double *grad_lid;    // dim*dim, += per column (MOVING sites)
+    double *tau_acc;     // per block: += dJ/domega of this launch's sites
+    const void *target;  // loss: u_x target on the plane, adjoint type, [x + z*dim]
+    double *loss_part;   // loss: per block partial sums
+    int dim;
+    int nvx;
+    unsigned nvec;
+    size_t n;
+    double omega;        // 1/tau in the forward's precision
+    double dloss;        // loss-gradient seed scale (dJ/dL * 2 / M)
+    int plane_y;         // loss plane
+};
+
+template <class S> struct AdjType { using type = float; };
+template <> struct AdjType<double> { using type = double; };
+
+// forward storage element -> value in the adjoint precision
+template <class S, class A> __device__ __forceinline__ A fwd_value(S v, int i)
+{
+    if constexpr (is_dev16<S>()) return (A)(wf_of(i) + Dev16<S>::to_f(v) * Dev16<S>::inv_scale);
+    else return (A)v;
+}
+
+template <class A>
+__device__ __forceinline__ void moments_plain(const A (&g)[Q], A &rho, A &ux, A &uy, A &uz)
+{
+    rho = 0;
+    A jx = 0, jy = 0, jz = 0;
+#pragma unroll
+    for (int i = 0; i < Q; ++i) {
+        rho += g[i];
+        if (ex_of(i)) jx += ex_of(i) > 0 ? g[i] : -g[i];
+        if (ey_of(i)) jy += ey_of(i) > 0 ? g[i] : -g[i];
+        if (ez_of(i)) jz += ez_of(i) > 0 ? g[i] : -g[i];
+    }
+    const A inv = (A)1 / rho;
+    ux = jx * inv;
+    uy = jy * inv;
+    uz = jz * inv;
+}
+
+template <class A> __device__ __forceinline__ A w_of(int i)
+{
+    return wclass_of(i) == 0 ? (A)1 / (A)3 : (wclass_of(i) == 1 ? (A)1 / (A)18 : (A)1 / (A)36);
+}
+
+// FLUID site: b (pulled adjoint) -> a (adjoint of the pre-collision values) in place.
+template <class A>
+__device__ __forceinline__ void adjoint_fluid(const A (&g)[Q], A (&b)[Q], A omega, A &dw)
+{
+    A rho, ux, uy, uz;
+    moments_plain(g, rho, ux, uy, uz);
+    const A u2 = ux * ux + uy * uy + uz * uz;
+    A B0 = 0, SB = 0, Gx = 0, Gy = 0, Gz = 0, d = 0;
+#pragma unroll
+    for (int i = 0; i < Q; ++i) {
+        const A eu = (A)ex_of(i) * ux + (A)ey_of(i) * uy + (A)ez_of(i) * uz;
+        const A w = w_of<A>(i);
+        const A p = (A)1 + (A)3 * eu + (A)4.5 * eu * eu - (A)1.5 * u2;
+        const A bw = b[i] * w;
+        B0 += bw * p;
+        SB += bw;
+        const A q = bw * ((A)3 + (A)9 * eu);
+        Gx += q * (A)ex_of(i);
+        Gy += q * (A)ey_of(i);
+        Gz += q * (A)ez_of(i);
+        d += b[i] * (w * rho * p - g[i]);
+    }
+    Gx -= (A)3 * ux * SB;
+    Gy -= (A)3 * uy * SB;
+    Gz -= (A)3 * uz * SB;
+    const A c = B0 - (Gx * ux + Gy * uy + Gz * uz);
+    const A keep = (A)1 - omega;
+#pragma unroll
+    for (int j = 0; j < Q; ++j)
+        b[j] = keep * b[j] + omega * (c + Gx * (A)ex_of(j) + Gy * (A)ey_of(j) + Gz * (A)ez_of(j));
+    dw += d;
+}
+
+// MOVING site.
+template <class A>
+__device__ __forceinline__ void adjoint_moving(const A (&g)[Q], A (&b)[Q], A lid, A &dlid)
+{
+    A rho = 0;
+#pragma unroll
+    for (int i = 0; i < Q; ++i) {
+        const bool replaced = (i == 5 || i == 11 || i == 12 || i == 13 || i == 14);
+        rho += replaced ? g[opp_of(i)] : g[i];
+    }
+    const A c15 = (A)1.5 * lid * lid;
+    A s = 0, dl = 0;
+#pragma unroll
+    for (int i = 0; i < Q; ++i) {
+        const A ex = (A)ex_of(i);
+        const A eu = ex * lid;
+        const A w = w_of<A>(i);
+        s += b[i] * w * ((A)1 + (A)3 * eu + (A)4.5 * eu * eu - c15);
+        dl += b[i] * w * rho * ((A)3 * ex + ((A)9 * ex * ex - (A)3) * lid);
+    }
+#pragma unroll
+    for (int j = 0; j < Q; ++j) {
+        const bool zero = (j == 5 || j == 11 || j == 12 || j == 13 || j == 14);
+        const bool twice = (j == 6 || j == 15 || j == 16 || j == 17 || j == 18);
+        b[j] = zero ? (A)0 : (twice ? (A)2 * s : s);
+    }
+    dlid += dl;
+}
+
+// One adjoint step a_{k+1} -> a_k over the interior rows; V sites per thread.
+template <class S>
+__global__ void __launch_bounds__(256) adjoint_kernel(AdjArgs a)
+{
+    using A = typename AdjType<S>::type;
+    using C = typename Compute<S>::type;
+    constexpr int V = 16 / (int)sizeof(A);
+    const unsigned g0 = blockIdx.x * blockDim.x + threadIdx.x;
+    A dw = 0;
+    if (g0 < a.nvec) {
+        const int dim = a.dim;
+        const unsigned row = g0 / (unsigned)a.nvx;
+        const int xv = (int)(g0 - row * (unsigned)a.nvx);
+        const int y = 1 + (int)(row % (unsigned)(dim - 2));
+        const int z = 1 + (int)(row / (unsigned)(dim - 2));
+        const int x0 = xv * V;
+        const size_t rowoff = (size_t)z * dim * dim + (size_t)y * dim;
+        const size_t site0 = rowoff + (size_t)x0;
+        const typename MapWord<V>::type mw =
+            __ldg(reinterpret_cast<const typename MapWord<V>::type *>(a.map + site0));
+
+        // reverse streaming: slot i of site s takes a_{k+1}(s + e_i, i)
+        const A *ain = static_cast<const A *>(a.ain);
+        A bs[Q][V];
+#pragma unroll
+        for (int i = 0; i < Q; ++i) {
+            const ptrdiff_t shift = (ptrdiff_t)ez_of(i) * dim * dim + (ptrdiff_t)ey_of(i) * dim;
+            const A *src = ain + (size_t)i * a.n + rowoff + shift;
+            if (ex_of(i) == 1) gather_row<A, V, -1>(src, x0, dim, bs[i]);
+            else if (ex_of(i) == -1) gather_row<A, V, 1>(src, x0, dim, bs[i]);
+            else gather_row<A, V, 0>(src, x0, dim, bs[i]);
+        }
+        // forward pre-collision values R_k(s): the forward pull
+        const S *fwd = static_cast<const S *>(a.fwd);
+        S fsv[Q][V];
+        gather_all<S, V, 0>(fwd, a.n, rowoff, dim, x0, fsv);
+
+        const C *lid = static_cast<const C *>(a.lid);
+        const A omega = (A)a.omega;
+        const Weights<C> W = make_weights<C>();
+#pragma unroll
+        for (int k = 0; k < V; ++k) {
+            const uint8_t b8 = (uint8_t)(mw >> (8 * k));
+            A g[Q], b[Q];
+#pragma unroll
+            for (int i = 0; i < Q; ++i) {
+                g[i] = fwd_value<S, A>(fsv[i][k], i);
+                b[i] = bs[i][k];
+            }
+            if (b8 & M_WALL) {
+#pragma unroll
+                for (int i = 0; i < Q; ++i) b[i] = (A)0;
+            } else if (b8 == 0) {
+                adjoint_fluid<A>(g, b, omega, dw);
+            } else {
+                // wall-sourced slots hold the site's initial equilibrium
+                const C lidv = (b8 & M_FRONT) ? lid[(size_t)y * dim + x0 + k] : (C)0;
+#pragma unroll
+                for (int i = 0; i < Q; ++i)
+                    if (wall_sourced(i, b8))
+                        g[i] = (A)((b8 & M_FRONT) ? (C)init_eq_exact<C>(i, lidv, W) : W.w[wclass_of(i)]);
+                if (b8 == M_FRONT) {
+                    A dl = 0;
+                    adjoint_moving<A>(g, b, (A)lidv, dl);
+                    a.grad_lid[(size_t)y * dim + x0 + k] += (double)dl;
+                } else if (!(b8 & M_CORNER)) {
+                    A t[Q];
+#pragma unroll
+                    for (int i = 0; i < Q; ++i) t[i] = b[opp_of(i)];
+#pragma unroll
+                    for (int i = 0; i < Q; ++i) b[i] = t[i];
+                }
+            }
+#pragma unroll
+            for (int i = 0; i < Q; ++i) bs[i][k] = b[i];
+        }
+        A *aout = static_cast<A *>(a.aout);
+#pragma unroll
+        for (int i = 0; i < Q; ++i) store_vec<A, V>(aout + (size_t)i * a.n + site0, bs[i]);
+    }
+    block_reduce_add((double)dw, a.tau_acc);
+}
+
+// Seed of the backward sweep: a_T = dJ/dR_T for the mid-plane loss
+//   J = (1/M) sum over the FLUID sites of plane y = plane_y of (u_x - target)^2,
+// dJ/dR_T(s, i) = (2/M) (u_x - target) (e_ix - u_x) / rho; zero elsewhere.
+// a.dloss carries the factor dJ_total/dJ * 2 / M.  Also writes the loss
+// partials (sum of squared differences) when loss_part != NULL.
+template <class S>
+__global__ void __launch_bounds__(256) loss_seed_kernel(AdjArgs a)
+{
+    using A = typename AdjType<S>::type;
+    const int dim = a.dim;
+    const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    double sq = 0.0;
+    if (id < a.n) {
+        const int x = (int)(id % dim), y = (int)((id / dim) % dim), z = (int)(id / ((size_t)dim * dim));
+        const bool on = y == a.plane_y && pack_cell(dim, x, y, z) == 0;
+        A *aout = static_cast<A *>(a.aout);
+        A out[Q];
+#pragma unroll
+        for (int i = 0; i < Q; ++i) out[i] = (A)0;
+        if (on) {
+            const S *fwd = static_cast<const S *>(a.fwd);
+            A g[Q];
+#pragma unroll
+            for (int i = 0; i < Q; ++i) {
+                const size_t src = id - (ptrdiff_t)ex_of(i) - (ptrdiff_t)ey_of(i) * dim - (ptrdiff_t)ez_of(i) * dim * dim;
+                g[i] = fwd_value<S, A>(fwd[(size_t)i * a.n + src], i);
+            }
+            A rho, ux, uy, uz;
+            moments_plain(g, rho, ux, uy, uz);
+            const A tgt = static_cast<const A *>(a.target)[(size_t)x + (size_t)z * dim];
+            const A diff = ux - tgt;
+            sq = (double)diff * (double)diff;
+            const A d = (A)a.dloss * diff / rho;
+#pragma unroll
+            for (int i = 0; i < Q; ++i) out[i] = d * ((A)ex_of(i) - ux);
+        }
+        if (aout) {
+#pragma unroll
+            for (int i = 0; i < Q; ++i) aout[(size_t)i * a.n + id] = out[i];
+        }
+    }
+    if (a.loss_part) block_reduce_write(sq, 0.0, a.loss_part);
+}
+
+// Lid sensitivity of an initial state made by the init kernel: the FRONT
+// sites (x, y in [1, dim-2], z = dim-2) start at the equilibrium at rho = 1
+// and u = (lid, 0, 0) (kernels.cl:292-308); dR_0(s,i)/dlid =
+// w_i (3 e_ix + (9 e_ix^2 - 3) lid).
+template <class S>
+__global__ void lid_init_grad_kernel(AdjArgs a)
+{
+    using A = typename AdjType<S>::type;
+    using C = typename Compute<S>::type;
+    const int dim = a.dim;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= dim * dim) return;
+    const int x = k % dim, y = k / dim;
+    if (x < 1 || y < 1 || x > dim - 2 || y > dim - 2) return;
+    const size_t id = (size_t)x + (size_t)y * dim + (size_t)(dim - 2) * dim * dim;
+    const A *a0 = static_cast<const A *>(a.ain);
+    const A lid = (A) static_cast<const C *>(a.lid)[k];
+    double s = 0.0;
+#pragma unroll
+    for (int i = 0; i < Q; ++i) {
+        const A ex = (A)ex_of(i);
+        s += (double)(a0[(size_t)i * a.n + id] * w_of<A>(i) * ((A)3 * ex + ((A)9 * ex * ex - (A)3) * lid));
+    }
+    a.grad_lid[k] += s;
+}
+
+// Adjoint buffer (post-stream layout) -> CSoA order of the F dumps.
+template <class A>
+__global__ void export_adjoint_kernel(const A *__restrict__ adj, A *__restrict__ out, size_t o0, size_t count, int sd,
+                                      size_t n)
+{
+    const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    size_t id;
+    int q;
+    decode_csoa(o0 + k, sd, n, id, q);
+    out[k] = adj[(size_t)q * n + id];
+}
+
+}  // namespace lbm

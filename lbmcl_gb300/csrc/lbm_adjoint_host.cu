@@ -1,0 +1,369 @@
+// lbm_adjoint_host.cu -- gradients of a mid-plane velocity loss with respect
+// to the lid-velocity profile, the relaxation time and the initial
+// populations (lbm_adjoint_* in include/lbm.h).
+//
+// lbm_adjoint_forward runs T iterations from the handle's current state,
+// keeping checkpoints Q_0, Q_c, Q_2c, ... of the P buffer (c = checkpoint
+// interval; c = 1 keeps the whole trajectory).  lbm_adjoint_backward seeds
+// a_T = dJ/dR_T, then walks the segments backwards: it restores a
+// checkpoint, recomputes the segment's intermediate states with the forward
+// kernel, and applies the adjoint step from the segment's last iteration to
+// its first.  Memory: ceil(T/c) checkpoints + (c - 1) segment states, i.e.
+// about 2 sqrt(T) states for c = sqrt(T); one extra forward iteration per
+// iteration of the backward sweep.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "lbm.h"
+#include "lbm_adjoint.cuh"
+#include "lbm_handle.h"
+#include "lbm_launch.h"
+
+namespace {
+
+constexpr unsigned kAdjBlock = 128;
+constexpr unsigned kLossBlock = 256;
+
+int fail(int code, const char *fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    lbm::set_last_error(buf);
+    return code;
+}
+
+#define ADJ_CUDA(call)                                                                               \
+    do {                                                                                             \
+        cudaError_t e_ = (call);                                                                     \
+        if (e_ != cudaSuccess) {                                                                     \
+            cudaGetLastError();                                                                      \
+            return fail(e_ == cudaErrorMemoryAllocation ? LBM_ENOMEM : LBM_ECUDA, "%s: %s", #call,   \
+                        cudaGetErrorString(e_));                                                     \
+        }                                                                                            \
+    } while (0)
+
+size_t adj_bytes(int prec) { return prec == LBM_FP64 ? 8 : 4; }
+int adj_vec(int prec) { return (int)(16 / adj_bytes(prec)); }
+
+lbm::AdjArgs adj_args(const lbm_t *h)
+{
+    lbm::AdjArgs a = {};
+    a.map = h->map;
+    a.lid = h->lid;
+    a.grad_lid = h->adj.grad_lid;
+    a.tau_acc = h->adj.tau_acc;
+    a.target = h->adj.target;
+    a.dim = h->dim;
+    a.nvx = h->dim / adj_vec(h->prec);
+    a.nvec = (unsigned)((size_t)a.nvx * (size_t)(h->dim - 2) * (size_t)(h->dim - 2));
+    a.n = h->n;
+    a.omega = h->inv_tau;
+    a.plane_y = h->adj.plane_y;
+    return a;
+}
+
+template <class S>
+cudaError_t run_adjoint_step(const lbm::AdjArgs &a, unsigned grid, cudaStream_t s)
+{
+    lbm::adjoint_kernel<S><<<grid, kAdjBlock, 0, s>>>(a);
+    return cudaGetLastError();
+}
+template <class S>
+cudaError_t run_loss_seed(const lbm::AdjArgs &a, unsigned grid, cudaStream_t s)
+{
+    lbm::loss_seed_kernel<S><<<grid, kLossBlock, 0, s>>>(a);
+    return cudaGetLastError();
+}
+template <class S>
+cudaError_t run_lid_init_grad(const lbm::AdjArgs &a, cudaStream_t s)
+{
+    const int nc = a.dim * a.dim;
+    lbm::lid_init_grad_kernel<S><<<(nc + 255) / 256, 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t adjoint_step(const lbm_t *h, const lbm::AdjArgs &a)
+{
+    switch (h->prec) {
+    case LBM_FP32: return run_adjoint_step<float>(a, h->adj.adj_grid, h->stream);
+    case LBM_FP64: return run_adjoint_step<double>(a, h->adj.adj_grid, h->stream);
+    case LBM_FP16: return run_adjoint_step<__half>(a, h->adj.adj_grid, h->stream);
+    default: return run_adjoint_step<__nv_bfloat16>(a, h->adj.adj_grid, h->stream);
+    }
+}
+
+cudaError_t loss_seed(const lbm_t *h, const lbm::AdjArgs &a)
+{
+    switch (h->prec) {
+    case LBM_FP32: return run_loss_seed<float>(a, h->adj.loss_grid, h->stream);
+    case LBM_FP64: return run_loss_seed<double>(a, h->adj.loss_grid, h->stream);
+    case LBM_FP16: return run_loss_seed<__half>(a, h->adj.loss_grid, h->stream);
+    default: return run_loss_seed<__nv_bfloat16>(a, h->adj.loss_grid, h->stream);
+    }
+}
+
+cudaError_t lid_init_grad(const lbm_t *h, const lbm::AdjArgs &a)
+{
+    switch (h->prec) {
+    case LBM_FP32: return run_lid_init_grad<float>(a, h->stream);
+    case LBM_FP64: return run_lid_init_grad<double>(a, h->stream);
+    case LBM_FP16: return run_lid_init_grad<__half>(a, h->stream);
+    default: return run_lid_init_grad<__nv_bfloat16>(a, h->stream);
+    }
+}
+
+// number of FLUID sites on the loss plane
+double plane_sites(const lbm_t *h)
+{
+    const int y = h->adj.plane_y;
+    if (y < 2 || y > h->dim - 3) return 0.0;
+    const double m = (double)(h->dim - 4);
+    return m * m;
+}
+
+// Device allocation counted against the handle's max_device_bytes budget.
+int alloc_tracked(lbm_t *h, void **p, size_t bytes)
+{
+    const size_t cap = h->cfg.max_device_bytes;
+    if (cap > 0 && h->base_bytes + h->adj.bytes + bytes > cap)
+        return fail(LBM_ENOMEM, "adjoint: needs %zu more device bytes, budget is %zu", bytes, cap);
+    ADJ_CUDA(cudaMalloc(p, bytes));
+    h->adj.bytes += bytes;
+    return LBM_OK;
+}
+
+void free_tracked(lbm_t *h, void *p, size_t bytes)
+{
+    if (!p) return;
+    cudaFree(p);
+    h->adj.bytes -= bytes;
+}
+
+}  // namespace
+
+namespace lbm {
+void release_adjoint(lbm_t *h)
+{
+    lbm_adjoint_state &s = h->adj;
+    for (void *p : s.ckpt) cudaFree(p);
+    for (void *p : s.seg) cudaFree(p);
+    s.ckpt.clear();
+    s.seg.clear();
+    for (void *&p : s.adj) {
+        if (p) cudaFree(p);
+        p = nullptr;
+    }
+    for (void *p : {(void *)s.grad_lid, (void *)s.tau_acc, (void *)s.loss_part, s.target})
+        if (p) cudaFree(p);
+    s.grad_lid = nullptr;
+    s.tau_acc = nullptr;
+    s.loss_part = nullptr;
+    s.target = nullptr;
+    s.bytes = 0;
+    s.ready = false;
+}
+}  // namespace lbm
+
+extern "C" {
+
+int lbm_adjoint_set_loss(lbm_t *h, int plane_y, const double *target_ux)
+{
+    if (!h) return fail(LBM_EINVAL, "lbm_adjoint_set_loss: NULL handle");
+    if (plane_y < 2 || plane_y > h->dim - 3)
+        return fail(LBM_EINVAL, "lbm_adjoint_set_loss: plane_y %d must hold FLUID sites ([2, %d])", plane_y,
+                    h->dim - 3);
+    const size_t nc = (size_t)h->dim * h->dim;
+    const size_t ab = adj_bytes(h->prec);
+    if (!h->adj.target) {
+        int rc = alloc_tracked(h, &h->adj.target, nc * ab);
+        if (rc != LBM_OK) return rc;
+    }
+    std::vector<unsigned char> buf(nc * ab);
+    for (size_t k = 0; k < nc; ++k) {
+        const double v = target_ux ? target_ux[k] : 0.0;
+        if (ab == 8) memcpy(&buf[k * 8], &v, 8);
+        else { const float f = (float)v; memcpy(&buf[k * 4], &f, 4); }
+    }
+    ADJ_CUDA(cudaMemcpyAsync(h->adj.target, buf.data(), buf.size(), cudaMemcpyHostToDevice, h->stream));
+    ADJ_CUDA(cudaStreamSynchronize(h->stream));
+    h->adj.plane_y = plane_y;
+    return LBM_OK;
+}
+
+int lbm_adjoint_forward(lbm_t *h, int iterations, int checkpoint_every, double *loss)
+{
+    if (!h) return fail(LBM_EINVAL, "lbm_adjoint_forward: NULL handle");
+    if (iterations < 1 || checkpoint_every < 1)
+        return fail(LBM_EINVAL, "lbm_adjoint_forward: iterations and checkpoint_every must be >= 1");
+    if (h->adj.plane_y < 0) return fail(LBM_ESTATE, "lbm_adjoint_forward: call lbm_adjoint_set_loss first");
+    lbm_adjoint_state &s = h->adj;
+    const size_t fbytes = (size_t)lbm::Q * h->n * lbm::storage_bytes(h->prec);
+    // drop the previous run's state buffers (the target and work buffers stay)
+    for (void *p : s.ckpt) free_tracked(h, p, fbytes);
+    for (void *p : s.seg) free_tracked(h, p, fbytes);
+    s.ckpt.clear();
+    s.seg.clear();
+    s.ready = false;
+    const int c = std::min(checkpoint_every, iterations);
+    const int nck = (iterations + c - 1) / c;
+    for (int k = 0; k < nck; ++k) {
+        void *p = nullptr;
+        int rc = alloc_tracked(h, &p, fbytes);
+        if (rc != LBM_OK) return rc;
+        s.ckpt.push_back(p);
+    }
+    for (int k = 0; k < c - 1; ++k) {
+        void *p = nullptr;
+        int rc = alloc_tracked(h, &p, fbytes);
+        if (rc != LBM_OK) return rc;
+        s.seg.push_back(p);
+    }
+    s.iterations = iterations;
+    s.every = c;
+    s.init_state = h->state_is_init;
+
+    // Q_0, then the iterations, copying Q_{jc} into checkpoint j
+    ADJ_CUDA(cudaMemcpyAsync(s.ckpt[0], h->f[h->cur], fbytes, cudaMemcpyDeviceToDevice, h->stream));
+    for (int k = 0; k < iterations; ++k) {
+        ADJ_CUDA(lbm::launch_iteration(h, h->f[h->cur], h->f[h->cur ^ 1]));
+        h->cur ^= 1;
+        const int done = k + 1;
+        if (done < iterations && done % c == 0)
+            ADJ_CUDA(cudaMemcpyAsync(s.ckpt[done / c], h->f[h->cur], fbytes, cudaMemcpyDeviceToDevice, h->stream));
+    }
+    h->it += iterations;
+    h->state_is_init = false;
+
+    // loss of R_T = S(Q_T)
+    s.loss_grid = (unsigned)((h->n + kLossBlock - 1) / kLossBlock);
+    if (!s.loss_part) {
+        int rc = alloc_tracked(h, (void **)&s.loss_part, ((size_t)s.loss_grid + 1) * 2 * sizeof(double));
+        if (rc != LBM_OK) return rc;
+    }
+    lbm::AdjArgs a = adj_args(h);
+    a.fwd = h->f[h->cur];
+    a.aout = nullptr;
+    a.loss_part = s.loss_part;
+    ADJ_CUDA(loss_seed(h, a));
+    ADJ_CUDA(lbm::launch_sum_partials(s.loss_part, (int)s.loss_grid, s.loss_part + 2 * (size_t)s.loss_grid,
+                                      h->stream));
+    double sums[2];
+    ADJ_CUDA(cudaMemcpyAsync(sums, s.loss_part + 2 * (size_t)s.loss_grid, sizeof sums, cudaMemcpyDeviceToHost,
+                             h->stream));
+    ADJ_CUDA(cudaEventRecord(h->ev_last, h->stream));
+    ADJ_CUDA(cudaStreamSynchronize(h->stream));
+    const double m = plane_sites(h);
+    if (loss) *loss = m > 0 ? sums[0] / m : 0.0;
+    s.ready = true;
+    s.it_end = h->it;
+    return LBM_OK;
+}
+
+int lbm_adjoint_backward(lbm_t *h, double dloss, double *grad_tau, double *grad_lid, void *grad_f0,
+                         size_t grad_f0_bytes)
+{
+    if (!h) return fail(LBM_EINVAL, "lbm_adjoint_backward: NULL handle");
+    lbm_adjoint_state &s = h->adj;
+    if (!s.ready || s.it_end != h->it)
+        return fail(LBM_ESTATE, "lbm_adjoint_backward: no adjoint forward recorded for the current state");
+    const size_t ab = adj_bytes(h->prec);
+    const size_t abytes = (size_t)lbm::Q * h->n * ab;
+    if (grad_f0 && grad_f0_bytes != abytes)
+        return fail(LBM_EINVAL, "lbm_adjoint_backward: grad_f0 is %zu bytes, needs %zu", grad_f0_bytes, abytes);
+    const size_t nc = (size_t)h->dim * h->dim;
+    const unsigned agrid =
+        (unsigned)(((size_t)(h->dim / adj_vec(h->prec)) * (size_t)(h->dim - 2) * (size_t)(h->dim - 2) + kAdjBlock - 1) /
+                   kAdjBlock);
+    if (!s.adj[0]) {
+        int rc = alloc_tracked(h, &s.adj[0], abytes);
+        if (rc == LBM_OK) rc = alloc_tracked(h, &s.adj[1], abytes);
+        if (rc == LBM_OK) rc = alloc_tracked(h, (void **)&s.grad_lid, nc * sizeof(double));
+        if (rc != LBM_OK) return rc;
+    }
+    if (s.tau_acc && s.adj_grid != agrid) {
+        free_tracked(h, s.tau_acc, (size_t)s.adj_grid * sizeof(double));
+        s.tau_acc = nullptr;
+    }
+    if (!s.tau_acc) {
+        int rc = alloc_tracked(h, (void **)&s.tau_acc, (size_t)agrid * sizeof(double));
+        if (rc != LBM_OK) return rc;
+    }
+    s.adj_grid = agrid;
+    cudaStream_t st = h->stream;
+    ADJ_CUDA(cudaMemsetAsync(s.adj[0], 0, abytes, st));
+    ADJ_CUDA(cudaMemsetAsync(s.adj[1], 0, abytes, st));
+    ADJ_CUDA(cudaMemsetAsync(s.grad_lid, 0, nc * sizeof(double), st));
+    ADJ_CUDA(cudaMemsetAsync(s.tau_acc, 0, (size_t)agrid * sizeof(double), st));
+
+    // seed a_T
+    int cur = 0;
+    lbm::AdjArgs a = adj_args(h);
+    const double m = plane_sites(h);
+    a.fwd = h->f[h->cur];
+    a.aout = s.adj[cur];
+    a.loss_part = nullptr;
+    a.dloss = m > 0 ? dloss * 2.0 / m : 0.0;
+    ADJ_CUDA(loss_seed(h, a));
+
+    // segments, last to first
+    const int T = s.iterations, c = s.every;
+    const int nck = (T + c - 1) / c;
+    for (int j = nck - 1; j >= 0; --j) {
+        const int start = j * c, end = std::min(T, start + c);
+        for (int k = start + 1; k < end; ++k) {
+            const void *fin = (k - 1 == start) ? s.ckpt[j] : s.seg[k - 2 - start];
+            ADJ_CUDA(lbm::launch_iteration(h, fin, s.seg[k - 1 - start]));
+        }
+        for (int k = end - 1; k >= start; --k) {
+            lbm::AdjArgs b = adj_args(h);
+            b.fwd = (k == start) ? s.ckpt[j] : s.seg[k - 1 - start];
+            b.ain = s.adj[cur];
+            b.aout = s.adj[cur ^ 1];
+            ADJ_CUDA(adjoint_step(h, b));
+            cur ^= 1;
+        }
+    }
+    // a_0 = dJ/dR_0; the init kernel's lid dependence of R_0
+    if (s.init_state) {
+        lbm::AdjArgs b = adj_args(h);
+        b.ain = s.adj[cur];
+        ADJ_CUDA(lid_init_grad(h, b));
+    }
+    std::vector<double> tau(agrid);
+    ADJ_CUDA(cudaMemcpyAsync(tau.data(), s.tau_acc, agrid * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (grad_lid) ADJ_CUDA(cudaMemcpyAsync(grad_lid, s.grad_lid, nc * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (grad_f0) {
+        const size_t total = (size_t)lbm::Q * h->n;
+        const size_t chunk = std::min(total, (size_t)1 << 25);
+        for (size_t o0 = 0; o0 < total; o0 += chunk) {
+            const size_t cnt = std::min(chunk, total - o0);
+            const unsigned g = (unsigned)((cnt + 255) / 256);
+            if (ab == 8)
+                lbm::export_adjoint_kernel<double><<<g, 256, 0, st>>>(static_cast<const double *>(s.adj[cur]),
+                                                                       static_cast<double *>(h->stage), o0, cnt,
+                                                                       h->sd, h->n);
+            else
+                lbm::export_adjoint_kernel<float><<<g, 256, 0, st>>>(static_cast<const float *>(s.adj[cur]),
+                                                                      static_cast<float *>(h->stage), o0, cnt,
+                                                                      h->sd, h->n);
+            ADJ_CUDA(cudaGetLastError());
+            ADJ_CUDA(cudaMemcpyAsync((char *)grad_f0 + o0 * ab, h->stage, cnt * ab, cudaMemcpyDeviceToHost, st));
+        }
+    }
+    ADJ_CUDA(cudaEventRecord(h->ev_last, st));
+    ADJ_CUDA(cudaStreamSynchronize(st));
+    double dw = 0.0;
+    for (double v : tau) dw += v;
+    // omega = 1 / tau
+    if (grad_tau) *grad_tau = -h->inv_tau * h->inv_tau * dw;
+    return LBM_OK;
+}
+
+}  // extern "C"

@@ -18,6 +18,7 @@
 
 #include "lbm.h"
 #include "lbm_device.cuh"
+#include "lbm_handle.h"
 #include "lbm_launch.h"
 
 namespace {
@@ -45,8 +46,8 @@ int fail(int code, const char *fmt, ...)
         }                                                                                       \
     } while (0)
 
-size_t storage_bytes(int prec) { return prec == LBM_FP64 ? 8 : (prec == LBM_FP32 ? 4 : 2); }
-size_t macro_bytes(int prec) { return prec == LBM_FP64 ? 8 : 4; }
+using lbm::macro_bytes;
+using lbm::storage_bytes;
 int vec_len(int prec) { return (int)(16 / storage_bytes(prec)); }
 int dim_multiple(int prec) { return (prec == LBM_FP16 || prec == LBM_BF16) ? 8 : 4; }
 
@@ -89,41 +90,6 @@ cudaError_t launch_sum_partials(const double *partials, int nblocks, double *out
 void set_last_error(const char *msg) { g_err = msg; }
 }  // namespace lbm
 
-struct lbm_handle {
-    lbm_config cfg;
-    int dim = 0;
-    size_t n = 0;
-    int prec = 0;
-    int V = 4;
-    int sd = 0;             // log2 of the CSoA stride of F dumps
-    double inv_tau = 0;     // 1/tau rounded to the compute precision
-    float omega_f = 0;
-    void *f[2] = {nullptr, nullptr};
-    int cur = 0;            // f[cur] holds P_{t-1}
-    uint8_t *map = nullptr;
-    void *rho = nullptr;
-    void *u = nullptr;
-    void *lid = nullptr;
-    void *stage = nullptr;
-    double *partials = nullptr;
-    double *red_out = nullptr;
-    int *status = nullptr;
-    cudaStream_t stream = nullptr;
-    cudaEvent_t ev_first = nullptr, ev_last = nullptr;
-    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending;
-    std::vector<cudaEvent_t> spare;
-    double kernels_ms = 0;
-    int64_t it = 0;
-    unsigned block = 128;
-    unsigned nvec = 0;
-    unsigned grid = 0;
-    // staged variant (LBM_KERNEL_STAGED)
-    int kernel = LBM_KERNEL_DIRECT;
-    int rows = 1, gpp = 0, stages = 0;
-    unsigned ngroups = 0, sgrid = 0, sblock = 0;
-    size_t ssmem = 0;
-    std::string device_name;
-};
 
 namespace {
 
@@ -164,6 +130,7 @@ void release(lbm_t *h)
 {
     if (!h) return;
     if (h->stream) cudaStreamSynchronize(h->stream);
+    lbm::release_adjoint(h);
     for (void *p : {h->f[0], h->f[1], (void *)h->map, h->rho, h->u, h->lid, h->stage, (void *)h->partials,
                     (void *)h->red_out, (void *)h->status})
         if (p) cudaFree(p);
@@ -280,6 +247,16 @@ size_t dump_elem(int prec) { return prec == LBM_FP64 ? 8 : 4; }
 
 }  // namespace
 
+namespace lbm {
+cudaError_t launch_iteration(const lbm_t *h, const void *fin, void *fout)
+{
+    StepArgs a = step_args(h, h->cur);
+    a.fin = fin;
+    a.fout = fout;
+    return launch_pull(h, MODE_STEP, a);
+}
+}  // namespace lbm
+
 extern "C" {
 
 void lbm_config_default(lbm_config *c)
@@ -375,6 +352,7 @@ int lbm_init(lbm_t **out, const lbm_config *c)
     h->block = block;
     h->nvec = (unsigned)nvec;
     h->grid = (unsigned)grid;
+    h->base_bytes = need;
 
     // tau = 3 nu + 0.5 and 1/tau in the compute precision (kernels.cl:61-62)
     if (prec == LBM_FP64) {
@@ -472,6 +450,8 @@ int lbm_step(lbm_t *h, int nsteps, int macro_every)
     if (!h) return fail(LBM_EINVAL, "lbm_step: NULL handle");
     if (nsteps < 0 || macro_every < 0) return fail(LBM_EINVAL, "lbm_step: nsteps and macro_every must be >= 0");
     if (nsteps == 0) return LBM_OK;
+    h->state_is_init = false;
+    h->adj.ready = false;
     int rc = fold_events(h, h->pending.size() > 4096);
     if (rc != LBM_OK) return rc;
     const bool per_step = h->cfg.profile_steps != 0;
@@ -582,6 +562,8 @@ int lbm_load(lbm_t *h, int what, const void *src, size_t bytes)
         return fail(LBM_EINVAL, "lbm_load: only LBM_DUMP_F and LBM_DUMP_F_RAW can be loaded");
     const size_t want = lbm_size(h, what);
     if (bytes != want) return fail(LBM_EINVAL, "lbm_load: buffer is %zu bytes, needs %zu", bytes, want);
+    h->state_is_init = false;
+    h->adj.ready = false;
     if (what == LBM_DUMP_F_RAW) {
         LBM_CUDA(cudaMemcpyAsync(h->f[h->cur], src, bytes, cudaMemcpyHostToDevice, h->stream));
     } else {

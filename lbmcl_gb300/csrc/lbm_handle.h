@@ -1,0 +1,82 @@
+// lbm_handle.h -- the lattice handle behind the opaque lbm_t of include/lbm.h
+// (internal to the library; shared by lbm_capi.cu and lbm_adjoint_host.cu).
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "lbm.h"
+
+// State of an adjoint run (lbm_adjoint_forward / lbm_adjoint_backward).
+struct lbm_adjoint_state {
+    int iterations = 0;        // T of the last adjoint forward
+    int every = 0;             // checkpoint interval c
+    std::vector<void *> ckpt;  // Q_0, Q_c, Q_2c, ... (P buffers)
+    std::vector<void *> seg;   // recomputed Q_{jc+1} .. Q_{jc+c-1} of one segment
+    void *adj[2] = {nullptr, nullptr};  // adjoint ping-pong (post-stream layout)
+    double *grad_lid = nullptr;         // dim*dim
+    double *tau_acc = nullptr;          // per adjoint block
+    double *loss_part = nullptr;        // per loss block (2 doubles)
+    void *target = nullptr;             // dim*dim u_x target, adjoint type
+    unsigned adj_grid = 0, loss_grid = 0;
+    int plane_y = -1;
+    bool init_state = false;   // Q_0 was made by the init kernel (lid-dependent)
+    bool ready = false;        // a forward was recorded and Q_T is current
+    int64_t it_end = -1;       // handle iteration count when the forward ended
+    size_t bytes = 0;          // device bytes held by this state
+};
+
+struct lbm_handle {
+    lbm_config cfg;
+    int dim = 0;
+    size_t n = 0;
+    int prec = 0;
+    int V = 4;
+    int sd = 0;             // log2 of the CSoA stride of F dumps
+    double inv_tau = 0;     // 1/tau rounded to the compute precision
+    float omega_f = 0;
+    void *f[2] = {nullptr, nullptr};
+    int cur = 0;            // f[cur] holds P_{t-1}
+    uint8_t *map = nullptr;
+    void *rho = nullptr;
+    void *u = nullptr;
+    void *lid = nullptr;
+    void *stage = nullptr;
+    double *partials = nullptr;
+    double *red_out = nullptr;
+    int *status = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev_first = nullptr, ev_last = nullptr;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending;
+    std::vector<cudaEvent_t> spare;
+    double kernels_ms = 0;
+    int64_t it = 0;
+    unsigned block = 128;
+    unsigned nvec = 0;
+    unsigned grid = 0;
+    // staged variant (LBM_KERNEL_STAGED)
+    int kernel = LBM_KERNEL_DIRECT;
+    int rows = 1, gpp = 0, stages = 0;
+    unsigned ngroups = 0, sgrid = 0, sblock = 0;
+    size_t ssmem = 0;
+    std::string device_name;
+    bool state_is_init = true;  // the populations are what lbm_init made
+    size_t base_bytes = 0;      // device bytes lbm_init allocated
+    lbm_adjoint_state adj;
+};
+
+
+
+namespace lbm {
+// storage / macro / dump element sizes of a precision
+inline size_t storage_bytes(int prec) { return prec == LBM_FP64 ? 8 : (prec == LBM_FP32 ? 4 : 2); }
+inline size_t macro_bytes(int prec) { return prec == LBM_FP64 ? 8 : 4; }
+// launch one iteration P_out = C(S(P_in)) with the handle's kernel variant
+cudaError_t launch_iteration(const lbm_t *h, const void *fin, void *fout);
+// free the device memory of an adjoint state
+void release_adjoint(lbm_t *h);
+}  // namespace lbm

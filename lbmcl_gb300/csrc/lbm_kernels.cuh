@@ -341,6 +341,25 @@ __device__ __forceinline__ void block_reduce_write(double m, double e, double *p
     }
 }
 
+// Block sum of v added to acc[blockIdx.x] (one writer per slot and launch, so
+// successive launches with the same grid accumulate deterministically).
+__device__ __forceinline__ void block_reduce_add(double v, double *acc)
+{
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    __shared__ double sm[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) sm[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = (blockDim.x + 31) >> 5;
+        v = lane < nw ? sm[lane] : 0.0;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+        if (lane == 0) acc[blockIdx.x] += v;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // The fused pull-stream + collide iteration.
 // ---------------------------------------------------------------------------

@@ -1,0 +1,123 @@
+"""The hand-written adjoint against FP64 central finite differences, the
+stored-trajectory adjoint against the checkpointed one, and the autograd
+harness.  Small grids; FP64 handles unless stated."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def loss_of(capi, dim, iters, lid, tau, plane, target, prec="fp64", f0=None, seed=0, noise=0.0, stride=None):
+    with capi.Lattice(dim, velocity=0.0, precision=prec, lid=lid, tau=tau, seed=seed, noise_sigma=noise,
+                      stride=stride) as L:
+        if f0 is not None:
+            L.load_f(f0)
+        L.adjoint_set_loss(plane, target)
+        return L.adjoint_forward(iters, iters)
+
+
+def setup_case(dim=16, seed=2):
+    rng = np.random.default_rng(seed)
+    lid = 0.05 + 0.01 * rng.standard_normal(dim * dim)
+    target = 0.02 * rng.standard_normal(dim * dim)
+    return lid, target
+
+
+@pytest.mark.parametrize("every", [1, 7])
+def test_gradients_match_central_differences(capi, every):
+    dim, iters, tau, plane = 16, 60, 0.53, 8
+    lid, target = setup_case(dim)
+    with capi.Lattice(dim, velocity=0.0, precision="fp64", lid=lid, tau=tau, seed=4, noise_sigma=1e-4) as L:
+        L.adjoint_set_loss(plane, target)
+        J = L.adjoint_forward(iters, every)
+        g_tau, g_lid, _ = L.adjoint_backward(1.0, want_f0=False)
+    assert J > 0
+    h = 1e-6
+    # lid: a MOVING column, a column on a FRONT edge (init contribution only), one in the middle
+    for (x, y) in [(5, 7), (1, 6), (9, 9)]:
+        lp, lm = lid.copy(), lid.copy()
+        lp[x + y * dim] += h
+        lm[x + y * dim] -= h
+        fd = (loss_of(capi, dim, iters, lp, tau, plane, target, seed=4, noise=1e-4) -
+              loss_of(capi, dim, iters, lm, tau, plane, target, seed=4, noise=1e-4)) / (2 * h)
+        assert abs(g_lid[y, x] - fd) <= 1e-6 * max(abs(fd), 1e-3 * np.abs(g_lid).max()), (x, y, g_lid[y, x], fd)
+    fd = (loss_of(capi, dim, iters, lid, tau + h, plane, target, seed=4, noise=1e-4) -
+          loss_of(capi, dim, iters, lid, tau - h, plane, target, seed=4, noise=1e-4)) / (2 * h)
+    assert abs(g_tau - fd) <= 1e-6 * abs(fd), (g_tau, fd)
+
+
+def test_initial_population_gradient(capi):
+    dim, iters, tau, plane = 16, 40, 0.56, 7
+    lid, target = setup_case(dim, 3)
+    with capi.Lattice(dim, velocity=0.0, precision="fp64", lid=lid, tau=tau, stride=16) as L:
+        f0 = L.f()
+        L.adjoint_set_loss(plane, target)
+        L.load_f(f0)  # R_0 given explicitly: no lid dependence through the init
+        L.adjoint_forward(iters, 5)
+        _, _, g0 = L.adjoint_backward(1.0)
+    n = dim ** 3
+    h = 1e-6
+    rng = np.random.default_rng(8)
+    for _ in range(6):
+        x, y, z = rng.integers(2, dim - 2, size=3)
+        q = int(rng.integers(0, 19))
+        idx = x + y * dim + z * dim * dim
+        k = ((idx // 16) * 19 + q) * 16 + (idx & 15)
+        fp, fm = f0.copy(), f0.copy()
+        fp[k] += h
+        fm[k] -= h
+        fd = (loss_of(capi, dim, iters, lid, tau, plane, target, f0=fp, stride=16) -
+              loss_of(capi, dim, iters, lid, tau, plane, target, f0=fm, stride=16)) / (2 * h)
+        assert abs(g0[k] - fd) <= 1e-6 * max(abs(fd), 1e-3 * np.abs(g0).max()), (x, y, z, q, g0[k], fd)
+    assert np.isnan(g0).sum() == 0 and g0.shape == (19 * n,)
+
+
+def test_checkpointing_is_exact(capi):
+    """Recomputed segments reproduce the stored trajectory bit for bit."""
+    dim, iters = 24, 50
+    lid, target = setup_case(dim, 5)
+    out = []
+    for every in (1, 8, 50):
+        with capi.Lattice(dim, velocity=0.0, precision="fp32", lid=lid, tau=0.52, seed=1, noise_sigma=1e-4) as L:
+            L.adjoint_set_loss(12, target)
+            L.adjoint_forward(iters, every)
+            out.append(L.adjoint_backward(1.0))
+    for o in out[1:]:
+        assert o[0] == out[0][0]
+        np.testing.assert_array_equal(o[1], out[0][1])
+        np.testing.assert_array_equal(o[2], out[0][2])
+
+
+@pytest.mark.parametrize("prec", ["fp32", "fp16", "bf16"])
+def test_fp32_adjoint_close_to_fp64(capi, prec):
+    dim, iters, plane = 24, 80, 12
+    lid, target = setup_case(dim, 6)
+    res = {}
+    for p in ("fp64", prec):
+        with capi.Lattice(dim, velocity=0.0, precision=p, lid=lid, tau=0.55, seed=2, noise_sigma=1e-4) as L:
+            L.adjoint_set_loss(plane, target)
+            L.adjoint_forward(iters, 10)
+            res[p] = L.adjoint_backward(1.0, want_f0=False)
+    g64, g = res["fp64"], res[prec]
+    tol = {"fp32": 1e-4, "fp16": 5e-2, "bf16": 2e-1}[prec]
+    assert abs(g[0] - g64[0]) <= tol * abs(g64[0])
+    assert np.linalg.norm(g[1] - g64[1]) <= tol * np.linalg.norm(g64[1])
+
+
+def test_autograd_harness(capi):
+    torch = pytest.importorskip("torch")
+    from lbmcl_gb300.adjoint import cavity_loss
+    dim, iters, plane = 16, 30, 8
+    lid0, target = setup_case(dim, 9)
+    lid = torch.tensor(lid0.reshape(dim, dim), dtype=torch.float64, requires_grad=True)
+    tau = torch.tensor(0.54, dtype=torch.float64, requires_grad=True)
+    J = cavity_loss(lid, tau, None, dim=dim, iterations=iters, plane_y=plane, target=target, checkpoint_every=6,
+                    precision="fp64")
+    (3.0 * J).backward()
+    with capi.Lattice(dim, velocity=0.0, precision="fp64", lid=lid0, tau=0.54) as L:
+        L.adjoint_set_loss(plane, target)
+        J2 = L.adjoint_forward(iters, iters)
+        g_tau, g_lid, _ = L.adjoint_backward(3.0, want_f0=False)
+    assert abs(float(J) - J2) <= 1e-15 * abs(J2)
+    np.testing.assert_allclose(lid.grad.numpy(), g_lid, rtol=1e-12, atol=0)
+    assert abs(float(tau.grad) - g_tau) <= 1e-12 * abs(g_tau)
