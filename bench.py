@@ -177,6 +177,49 @@ def time_e2e(capi, prec, steps, device):
     return (t1 - t0) * 1e3, h2d, d2h
 
 
+ADJOINT = dict(dim=256, viscosity=0.0089, velocity=0.05, iterations=400, checkpoint_every=20, plane_y=128)
+
+
+def time_adjoint(capi, prec, device):
+    """Adjoint/forward time at 256^3: the plain forward iteration against
+    the backward sweep of lbm_adjoint_backward (checkpoint segments
+    recomputed + hand-written adjoint kernel), per iteration, with the
+    checkpointed forward reported too."""
+    import torch
+    a = ADJOINT
+    dim, T, c = a["dim"], a["iterations"], a["checkpoint_every"]
+    rng = np.random.default_rng(7)
+    lid = 0.05 + 0.005 * rng.standard_normal(dim * dim)
+    target = 0.01 * rng.standard_normal(dim * dim)
+    with capi.Lattice(dim, a["viscosity"], a["velocity"], precision=prec, lid=lid, seed=3, noise_sigma=1e-4,
+                      device=device) as L:
+        stream = torch.cuda.ExternalStream(L.stream, device=device)
+        L.step(5)
+        L.sync()
+        e0, e1 = _events()
+        e0.record(stream)
+        L.step(T)
+        e1.record(stream)
+        e1.synchronize()
+        fwd_ms = e0.elapsed_time(e1) / T
+        L.adjoint_set_loss(a["plane_y"], target)
+        torch.cuda.synchronize(device)
+        t0 = time.perf_counter()
+        L.adjoint_forward(T, c)
+        t1 = time.perf_counter()
+        L.adjoint_backward(1.0, want_f0=False)
+        t2 = time.perf_counter()
+        mem = torch.cuda.mem_get_info(device)
+    ckpt_ms = (t1 - t0) * 1e3 / T
+    bwd_ms = (t2 - t1) * 1e3 / T
+    return {"dim": dim, "storage": prec, "adjoint": "fp32" if prec != "fp64" else "fp64", "iterations": T,
+            "checkpoint_every": c, "forward_ms_per_iter": round(fwd_ms, 4),
+            "checkpointed_forward_ms_per_iter": round(ckpt_ms, 4), "backward_ms_per_iter": round(bwd_ms, 4),
+            "adjoint_over_forward": round(bwd_ms / fwd_ms, 3),
+            "forward_plus_backward_over_forward": round((ckpt_ms + bwd_ms) / fwd_ms, 3),
+            "device_free_gb_during": round(mem[0] / 1e9, 1)}
+
+
 def traffic_from_profiles(prec):
     """DRAM bytes per launch from the committed ncu summary, scaled to 512^3."""
     p = os.path.join(ROOT, "profiles", f"pull_{prec}.txt")
@@ -271,6 +314,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint/forward leg")
     ap.add_argument("--modes", default="fp16,bf16,fp32,fp64")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -315,6 +359,9 @@ def main():
 
     head = modes[0]
     ms_head = res[head]["ms_per_step"]
+    adjoint = None
+    if not args.no_adjoint:
+        adjoint = {p: time_adjoint(capi, p, device) for p in ("fp16", "fp32")}
     e2e_ms, h2d, d2h = time_e2e(capi, head, args.steps, device)
     e2e_mlups = wet * args.steps / (e2e_ms * 1e3) * ws
 
@@ -340,6 +387,7 @@ def main():
             "modes": res,
             "ratio_fp16_vs_fp32": round(res["fp16"]["mlups"] / res["fp32"]["mlups"], 3)
             if "fp16" in res and "fp32" in res else None,
+            "adjoint": adjoint,
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
                          "kernel": "pull_kernel, one iteration = interior-row launch + face-row launch",

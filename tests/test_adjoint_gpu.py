@@ -121,6 +121,6 @@ def test_autograd_harness(capi):
         L.adjoint_set_loss(plane, target)
         J2 = L.adjoint_forward(iters, iters)
         g_tau, g_lid, _ = L.adjoint_backward(3.0, want_f0=False)
-    assert abs(float(J) - J2) <= 1e-15 * abs(J2)
+    assert abs(float(J.detach()) - J2) <= 1e-15 * abs(J2)
     np.testing.assert_allclose(lid.grad.numpy(), g_lid, rtol=1e-12, atol=0)
     assert abs(float(tau.grad) - g_tau) <= 1e-12 * abs(g_tau)
