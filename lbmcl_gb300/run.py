@@ -24,6 +24,8 @@ def main(argv=None) -> int:
     ap.add_argument("--block", type=int, default=0)
     ap.add_argument("--kernel", default="auto", choices=sorted(capi.KERNELS))
     ap.add_argument("--stages", type=int, default=0)
+    ap.add_argument("--adjoint", default="", help="T,c: also run an adjoint forward/backward of T iterations, "
+                                                  "checkpoint every c")
     a = ap.parse_args(argv)
     with capi.Lattice(a.dim, a.viscosity, a.velocity, precision=a.precision, stride=0, seed=a.seed,
                       noise_sigma=a.noise, block_threads=a.block, profile_steps=True, kernel=a.kernel,
@@ -34,6 +36,16 @@ def main(argv=None) -> int:
         wall = time.perf_counter() - t0
         total_ms, kernels_ms = L.timing()
         mass, energy, count = L.reduce()
+        if a.adjoint:
+            T, c = (int(v) for v in a.adjoint.split(","))
+            L.adjoint_set_loss(a.dim // 2, None)
+            t0 = time.perf_counter()
+            J = L.adjoint_forward(T, c)
+            t1 = time.perf_counter()
+            g_tau, g_lid, _ = L.adjoint_backward(1.0, want_f0=False)
+            t2 = time.perf_counter()
+            print(f"adjoint T={T} c={c} loss={J:.6e} forward={1e3 * (t1 - t0) / T:.4f} ms/iter "
+                  f"backward={1e3 * (t2 - t1) / T:.4f} ms/iter dJ/dtau={g_tau:.6e}")
     wet = (a.dim - 2) ** 3
     print(f"dim={a.dim} precision={a.precision} steps={a.steps} kernels={kernels_ms:.3f} ms "
           f"kernel MLUPS={wet * a.steps / (kernels_ms * 1e3):.1f} wall={wall * 1e3:.1f} ms "
