@@ -48,6 +48,7 @@ struct AdjArgs {
     double omega;        // 1/tau in the forward's precision
     double dloss;        // loss-gradient seed scale (dJ/dL * 2 / M)
     int plane_y;         // loss plane
+    unsigned tau_base;   // first tau_acc slot of this launch
 };
 
 template <class S> struct AdjType { using type = float; };
@@ -83,39 +84,6 @@ template <class A> __device__ __forceinline__ A w_of(int i)
     return wclass_of(i) == 0 ? (A)1 / (A)3 : (wclass_of(i) == 1 ? (A)1 / (A)18 : (A)1 / (A)36);
 }
 
-// FLUID site: b (pulled adjoint) -> a (adjoint of the pre-collision values) in place.
-template <class A>
-__device__ __forceinline__ void adjoint_fluid(const A (&g)[Q], A (&b)[Q], A omega, A &dw)
-{
-    A rho, ux, uy, uz;
-    moments_plain(g, rho, ux, uy, uz);
-    const A u2 = ux * ux + uy * uy + uz * uz;
-    A B0 = 0, SB = 0, Gx = 0, Gy = 0, Gz = 0, d = 0;
-#pragma unroll
-    for (int i = 0; i < Q; ++i) {
-        const A eu = (A)ex_of(i) * ux + (A)ey_of(i) * uy + (A)ez_of(i) * uz;
-        const A w = w_of<A>(i);
-        const A p = (A)1 + (A)3 * eu + (A)4.5 * eu * eu - (A)1.5 * u2;
-        const A bw = b[i] * w;
-        B0 += bw * p;
-        SB += bw;
-        const A q = bw * ((A)3 + (A)9 * eu);
-        Gx += q * (A)ex_of(i);
-        Gy += q * (A)ey_of(i);
-        Gz += q * (A)ez_of(i);
-        d += b[i] * (w * rho * p - g[i]);
-    }
-    Gx -= (A)3 * ux * SB;
-    Gy -= (A)3 * uy * SB;
-    Gz -= (A)3 * uz * SB;
-    const A c = B0 - (Gx * ux + Gy * uy + Gz * uz);
-    const A keep = (A)1 - omega;
-#pragma unroll
-    for (int j = 0; j < Q; ++j)
-        b[j] = keep * b[j] + omega * (c + Gx * (A)ex_of(j) + Gy * (A)ey_of(j) + Gz * (A)ez_of(j));
-    dw += d;
-}
-
 // MOVING site.
 template <class A>
 __device__ __forceinline__ void adjoint_moving(const A (&g)[Q], A (&b)[Q], A lid, A &dlid)
@@ -145,26 +113,147 @@ __device__ __forceinline__ void adjoint_moving(const A (&g)[Q], A (&b)[Q], A lid
     dlid += dl;
 }
 
-// One adjoint step a_{k+1} -> a_k over the interior rows; V sites per thread.
-template <class S>
-__global__ void __launch_bounds__(256) adjoint_kernel(AdjArgs a)
+// FLUID adjoint written around opposite pairs (i, i') with e_i.u = +-a:
+//   p_(+-) = base +- 3a, base = 1 + 4.5 a^2 - 1.5 u^2
+//   B0 = sum_c w_c sum_pairs (s base + 3 a d),   s = b+ + b-, d = b+ - b-
+//   G  = sum_c w_c sum_pairs e_i (3 d + 9 a s) - 3 u SB,  SB = sum_c w_c sum s
+//   a_(+-) = (1 - omega) b_(+-) + omega (B0 - G.u) +- omega G.e_i
+//   dJ/domega += rho B0 - sum_i b_i g_i
+template <class A>
+__device__ __forceinline__ void adjoint_fluid_pairs(const A (&g)[Q], A (&b)[Q], A omega, A &dw)
+{
+    A rho = 0, jx = 0, jy = 0, jz = 0, bg = 0;
+#pragma unroll
+    for (int i = 0; i < Q; ++i) {
+        rho += g[i];
+        if (ex_of(i)) jx += ex_of(i) > 0 ? g[i] : -g[i];
+        if (ey_of(i)) jy += ey_of(i) > 0 ? g[i] : -g[i];
+        if (ez_of(i)) jz += ez_of(i) > 0 ? g[i] : -g[i];
+        bg += b[i] * g[i];
+    }
+    const A inv = (A)1 / rho;
+    const A ux = jx * inv, uy = jy * inv, uz = jz * inv;
+    const A c0 = (A)1 - (A)1.5 * (ux * ux + uy * uy + uz * uz);
+    // per weight class accumulators: rest (0), axis (1), edge (2)
+    A B[3] = {b[0] * c0, 0, 0}, SB[3] = {b[0], 0, 0};
+    A Gx[3] = {0, 0, 0}, Gy[3] = {0, 0, 0}, Gz[3] = {0, 0, 0};
+    // (i, i') pairs with e_i listed first
+    constexpr int P[9][2] = {{1, 3}, {2, 4}, {6, 5}, {7, 9}, {8, 10}, {11, 17}, {12, 18}, {15, 13}, {16, 14}};
+    A av[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+        const int i = P[k][0], j = P[k][1];
+        const int c = wclass_of(i);
+        const A aa = (A)ex_of(i) * ux + (A)ey_of(i) * uy + (A)ez_of(i) * uz;
+        av[k] = aa;
+        const A sm = b[i] + b[j], df = b[i] - b[j];
+        B[c] += sm * (c0 + (A)4.5 * aa * aa) + (A)3 * aa * df;
+        SB[c] += sm;
+        const A q = (A)3 * df + (A)9 * aa * sm;
+        if (ex_of(i)) Gx[c] += ex_of(i) > 0 ? q : -q;
+        if (ey_of(i)) Gy[c] += ey_of(i) > 0 ? q : -q;
+        if (ez_of(i)) Gz[c] += ez_of(i) > 0 ? q : -q;
+    }
+    const A w0 = w_of<A>(0), w1 = w_of<A>(1), w2 = w_of<A>(2);
+    const A B0 = w0 * B[0] + w1 * B[1] + w2 * B[2];
+    const A sb = w0 * SB[0] + w1 * SB[1] + w2 * SB[2];
+    const A gx = w1 * Gx[1] + w2 * Gx[2] - (A)3 * ux * sb;
+    const A gy = w1 * Gy[1] + w2 * Gy[2] - (A)3 * uy * sb;
+    const A gz = w1 * Gz[1] + w2 * Gz[2] - (A)3 * uz * sb;
+    const A keep = (A)1 - omega;
+    const A oc = omega * (B0 - (gx * ux + gy * uy + gz * uz));
+    b[0] = keep * b[0] + oc;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+        const int i = P[k][0], j = P[k][1];
+        A ge = 0;
+        if (ex_of(i)) ge += ex_of(i) > 0 ? gx : -gx;
+        if (ey_of(i)) ge += ey_of(i) > 0 ? gy : -gy;
+        if (ez_of(i)) ge += ez_of(i) > 0 ? gz : -gz;
+        const A t = omega * ge;
+        b[i] = keep * b[i] + (oc + t);
+        b[j] = keep * b[j] + (oc - t);
+    }
+    dw += rho * B0 - bg;
+}
+
+// Any site kind (face rows): map-driven.  g gets the wall-sourced constants.
+template <class A, class C>
+__device__ __forceinline__ void adjoint_general(A (&g)[Q], A (&b)[Q], uint8_t b8, C lidv, A omega,
+                                                const Weights<C> &W, A &dw, A &dlid)
+{
+    if (b8 & M_WALL) {
+#pragma unroll
+        for (int i = 0; i < Q; ++i) b[i] = (A)0;
+        return;
+    }
+    if (b8 == 0) {
+        adjoint_fluid_pairs<A>(g, b, omega, dw);
+        return;
+    }
+#pragma unroll
+    for (int i = 0; i < Q; ++i)
+        if (wall_sourced(i, b8)) g[i] = (A)((b8 & M_FRONT) ? (C)init_eq_exact<C>(i, lidv, W) : W.w[wclass_of(i)]);
+    if (b8 == M_FRONT) {
+        adjoint_moving<A>(g, b, (A)lidv, dlid);
+    } else if (!(b8 & M_CORNER)) {
+        A t[Q];
+#pragma unroll
+        for (int i = 0; i < Q; ++i) t[i] = b[opp_of(i)];
+#pragma unroll
+        for (int i = 0; i < Q; ++i) b[i] = t[i];
+    }
+}
+
+// Adjoint of the x-face site xf of an interior row (bounce-back): a_j =
+// b_opp(j) = a_{k+1}(s - e_j, opp(j)), reloaded from the input adjoint.
+template <class A, int V>
+__device__ __forceinline__ void adjoint_face_fix(const AdjArgs &a, size_t rowoff, int xf, int k, A (&bs)[Q][V])
+{
+    const A *ain = static_cast<const A *>(a.ain);
+    const int dim = a.dim;
+#pragma unroll
+    for (int j = 0; j < Q; ++j) {
+        const int o = opp_of(j);
+        const ptrdiff_t shift = (ptrdiff_t)ez_of(j) * dim * dim + (ptrdiff_t)ey_of(j) * dim;
+        bs[j][k] = load_one(ain + (size_t)o * a.n + rowoff - shift + (xf - ex_of(j)));
+    }
+}
+
+// One adjoint step a_{k+1} -> a_k over the rows of one kind (ROWS_INTERIOR:
+// y, z in [2, dim-3], branch-free FLUID adjoint then the row ends patched;
+// ROWS_FACES: the general path).  V = VB / sizeof(A) sites per thread.
+// register cap of the adjoint kernels: 128 (two 256-thread blocks per SM)
+// for the FP32 adjoint, uncapped for FP64
+#ifndef LBM_ADJ_MINB
+#define LBM_ADJ_MINB 2
+#endif
+template <class S> constexpr int adj_min_blocks() { return sizeof(S) == 8 ? 1 : LBM_ADJ_MINB; }
+
+template <class S, int VB, int ROWS>
+__global__ void __launch_bounds__(256, adj_min_blocks<S>()) adjoint_kernel(AdjArgs a)
 {
     using A = typename AdjType<S>::type;
     using C = typename Compute<S>::type;
-    constexpr int V = 16 / (int)sizeof(A);
+    constexpr int V = VB / (int)sizeof(A);
+    const int dim = a.dim;
+    const int nvx = dim / V;
+    const unsigned nrows = ROWS == ROWS_INTERIOR ? (unsigned)(dim - 4) * (unsigned)(dim - 4) : 4u * (unsigned)(dim - 3);
     const unsigned g0 = blockIdx.x * blockDim.x + threadIdx.x;
     A dw = 0;
-    if (g0 < a.nvec) {
-        const int dim = a.dim;
-        const unsigned row = g0 / (unsigned)a.nvx;
-        const int xv = (int)(g0 - row * (unsigned)a.nvx);
-        const int y = 1 + (int)(row % (unsigned)(dim - 2));
-        const int z = 1 + (int)(row / (unsigned)(dim - 2));
+    if (g0 < nrows * (unsigned)nvx) {
+        const unsigned row = g0 / (unsigned)nvx;
+        const int xv = (int)(g0 - row * (unsigned)nvx);
+        int y, z;
+        if (ROWS == ROWS_INTERIOR) {
+            y = 2 + (int)(row % (unsigned)(dim - 4));
+            z = 2 + (int)(row / (unsigned)(dim - 4));
+        } else {
+            decode_face_row(dim, row, y, z);
+        }
         const int x0 = xv * V;
         const size_t rowoff = (size_t)z * dim * dim + (size_t)y * dim;
         const size_t site0 = rowoff + (size_t)x0;
-        const typename MapWord<V>::type mw =
-            __ldg(reinterpret_cast<const typename MapWord<V>::type *>(a.map + site0));
 
         // reverse streaming: slot i of site s takes a_{k+1}(s + e_i, i)
         const A *ain = static_cast<const A *>(a.ain);
@@ -181,51 +270,61 @@ __global__ void __launch_bounds__(256) adjoint_kernel(AdjArgs a)
         const S *fwd = static_cast<const S *>(a.fwd);
         S fsv[Q][V];
         gather_all<S, V, 0>(fwd, a.n, rowoff, dim, x0, fsv);
-
-        const C *lid = static_cast<const C *>(a.lid);
         const A omega = (A)a.omega;
-        const Weights<C> W = make_weights<C>();
+
+        if (ROWS == ROWS_INTERIOR) {
 #pragma unroll
-        for (int k = 0; k < V; ++k) {
-            const uint8_t b8 = (uint8_t)(mw >> (8 * k));
-            A g[Q], b[Q];
+            for (int k = 0; k < V; ++k) {
+                A g[Q], b[Q];
 #pragma unroll
-            for (int i = 0; i < Q; ++i) {
-                g[i] = fwd_value<S, A>(fsv[i][k], i);
-                b[i] = bs[i][k];
-            }
-            if (b8 & M_WALL) {
-#pragma unroll
-                for (int i = 0; i < Q; ++i) b[i] = (A)0;
-            } else if (b8 == 0) {
-                adjoint_fluid<A>(g, b, omega, dw);
-            } else {
-                // wall-sourced slots hold the site's initial equilibrium
-                const C lidv = (b8 & M_FRONT) ? lid[(size_t)y * dim + x0 + k] : (C)0;
-#pragma unroll
-                for (int i = 0; i < Q; ++i)
-                    if (wall_sourced(i, b8))
-                        g[i] = (A)((b8 & M_FRONT) ? (C)init_eq_exact<C>(i, lidv, W) : W.w[wclass_of(i)]);
-                if (b8 == M_FRONT) {
-                    A dl = 0;
-                    adjoint_moving<A>(g, b, (A)lidv, dl);
-                    a.grad_lid[(size_t)y * dim + x0 + k] += (double)dl;
-                } else if (!(b8 & M_CORNER)) {
-                    A t[Q];
-#pragma unroll
-                    for (int i = 0; i < Q; ++i) t[i] = b[opp_of(i)];
-#pragma unroll
-                    for (int i = 0; i < Q; ++i) b[i] = t[i];
+                for (int i = 0; i < Q; ++i) {
+                    g[i] = fwd_value<S, A>(fsv[i][k], i);
+                    b[i] = bs[i][k];
                 }
-            }
+                A d = 0;
+                adjoint_fluid_pairs<A>(g, b, omega, d);
+                // x in [2, dim-3] is FLUID; the row ends are patched below
+                if ((unsigned)(x0 + k - 2) <= (unsigned)(dim - 5)) dw += d;
 #pragma unroll
-            for (int i = 0; i < Q; ++i) bs[i][k] = b[i];
+                for (int i = 0; i < Q; ++i) bs[i][k] = b[i];
+            }
+            if (x0 == 0) {
+#pragma unroll
+                for (int i = 0; i < Q; ++i) bs[i][0] = (A)0;
+                adjoint_face_fix<A, V>(a, rowoff, 1, 1, bs);
+            }
+            if (x0 + V == dim) {
+#pragma unroll
+                for (int i = 0; i < Q; ++i) bs[i][V - 1] = (A)0;
+                adjoint_face_fix<A, V>(a, rowoff, dim - 2, V - 2, bs);
+            }
+        } else {
+            const typename MapWord<V>::type mw =
+                __ldg(reinterpret_cast<const typename MapWord<V>::type *>(a.map + site0));
+            const C *lid = static_cast<const C *>(a.lid);
+            const Weights<C> W = make_weights<C>();
+#pragma unroll
+            for (int k = 0; k < V; ++k) {
+                const uint8_t b8 = (uint8_t)(mw >> (8 * k));
+                A g[Q], b[Q];
+#pragma unroll
+                for (int i = 0; i < Q; ++i) {
+                    g[i] = fwd_value<S, A>(fsv[i][k], i);
+                    b[i] = bs[i][k];
+                }
+                const C lidv = (b8 & M_FRONT) ? lid[(size_t)y * dim + x0 + k] : (C)0;
+                A dl = 0;
+                adjoint_general<A, C>(g, b, b8, lidv, omega, W, dw, dl);
+                if (b8 == M_FRONT) a.grad_lid[(size_t)y * dim + x0 + k] += (double)dl;
+#pragma unroll
+                for (int i = 0; i < Q; ++i) bs[i][k] = b[i];
+            }
         }
         A *aout = static_cast<A *>(a.aout);
 #pragma unroll
         for (int i = 0; i < Q; ++i) store_vec<A, V>(aout + (size_t)i * a.n + site0, bs[i]);
     }
-    block_reduce_add((double)dw, a.tau_acc);
+    block_reduce_add((double)dw, a.tau_acc + a.tau_base);
 }
 
 // Seed of the backward sweep: a_T = dJ/dR_T for the mid-plane loss

@@ -50,7 +50,17 @@ int fail(int code, const char *fmt, ...)
     } while (0)
 
 size_t adj_bytes(int prec) { return prec == LBM_FP64 ? 8 : 4; }
-int adj_vec(int prec) { return (int)(16 / adj_bytes(prec)); }
+// adjoint kernels: 2 sites per thread (8-byte FP32 / 16-byte FP64 vectors)
+constexpr int kAdjV = 2;
+
+// blocks of the interior-row and face-row adjoint launches
+void adj_grids(const lbm_t *h, unsigned &gi, unsigned &gf)
+{
+    const size_t nvx = (size_t)(h->dim / kAdjV);
+    const size_t m = (size_t)(h->dim - 4);
+    gi = (unsigned)((m * m * nvx + kAdjBlock - 1) / kAdjBlock);
+    gf = (unsigned)((4 * (size_t)(h->dim - 3) * nvx + kAdjBlock - 1) / kAdjBlock);
+}
 
 lbm::AdjArgs adj_args(const lbm_t *h)
 {
@@ -61,7 +71,7 @@ lbm::AdjArgs adj_args(const lbm_t *h)
     a.tau_acc = h->adj.tau_acc;
     a.target = h->adj.target;
     a.dim = h->dim;
-    a.nvx = h->dim / adj_vec(h->prec);
+    a.nvx = h->dim / kAdjV;
     a.nvec = (unsigned)((size_t)a.nvx * (size_t)(h->dim - 2) * (size_t)(h->dim - 2));
     a.n = h->n;
     a.omega = h->inv_tau;
@@ -70,9 +80,18 @@ lbm::AdjArgs adj_args(const lbm_t *h)
 }
 
 template <class S>
-cudaError_t run_adjoint_step(const lbm::AdjArgs &a, unsigned grid, cudaStream_t s)
+cudaError_t run_adjoint_step(const lbm::AdjArgs &a0, unsigned gi, unsigned gf, cudaStream_t s)
 {
-    lbm::adjoint_kernel<S><<<grid, kAdjBlock, 0, s>>>(a);
+    constexpr int VB = kAdjV * (int)sizeof(typename lbm::AdjType<S>::type);
+    lbm::AdjArgs a = a0;
+    if (gi > 0) {
+        a.tau_base = 0;
+        lbm::adjoint_kernel<S, VB, lbm::ROWS_INTERIOR><<<gi, kAdjBlock, 0, s>>>(a);
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    a.tau_base = gi;
+    lbm::adjoint_kernel<S, VB, lbm::ROWS_FACES><<<gf, kAdjBlock, 0, s>>>(a);
     return cudaGetLastError();
 }
 template <class S>
@@ -91,11 +110,13 @@ cudaError_t run_lid_init_grad(const lbm::AdjArgs &a, cudaStream_t s)
 
 cudaError_t adjoint_step(const lbm_t *h, const lbm::AdjArgs &a)
 {
+    unsigned gi, gf;
+    adj_grids(h, gi, gf);
     switch (h->prec) {
-    case LBM_FP32: return run_adjoint_step<float>(a, h->adj.adj_grid, h->stream);
-    case LBM_FP64: return run_adjoint_step<double>(a, h->adj.adj_grid, h->stream);
-    case LBM_FP16: return run_adjoint_step<__half>(a, h->adj.adj_grid, h->stream);
-    default: return run_adjoint_step<__nv_bfloat16>(a, h->adj.adj_grid, h->stream);
+    case LBM_FP32: return run_adjoint_step<float>(a, gi, gf, h->stream);
+    case LBM_FP64: return run_adjoint_step<double>(a, gi, gf, h->stream);
+    case LBM_FP16: return run_adjoint_step<__half>(a, gi, gf, h->stream);
+    default: return run_adjoint_step<__nv_bfloat16>(a, gi, gf, h->stream);
     }
 }
 
@@ -278,9 +299,9 @@ int lbm_adjoint_backward(lbm_t *h, double dloss, double *grad_tau, double *grad_
     if (grad_f0 && grad_f0_bytes != abytes)
         return fail(LBM_EINVAL, "lbm_adjoint_backward: grad_f0 is %zu bytes, needs %zu", grad_f0_bytes, abytes);
     const size_t nc = (size_t)h->dim * h->dim;
-    const unsigned agrid =
-        (unsigned)(((size_t)(h->dim / adj_vec(h->prec)) * (size_t)(h->dim - 2) * (size_t)(h->dim - 2) + kAdjBlock - 1) /
-                   kAdjBlock);
+    unsigned gi, gf;
+    adj_grids(h, gi, gf);
+    const unsigned agrid = gi + gf;  // tau partial slots of the two launches
     if (!s.adj[0]) {
         int rc = alloc_tracked(h, &s.adj[0], abytes);
         if (rc == LBM_OK) rc = alloc_tracked(h, &s.adj[1], abytes);

@@ -32,13 +32,16 @@ template <class S> __host__ __device__ constexpr bool is_dev16() { return sizeof
 template <class S, int V>
 __device__ __forceinline__ void load_vec(const S *__restrict__ p, S (&out)[V])
 {
-    static_assert(V * sizeof(S) == 16 || V * sizeof(S) == 8, "8- or 16-byte vectors");
+    static_assert(V * sizeof(S) == 16 || V * sizeof(S) == 8 || V * sizeof(S) == 4, "4-, 8- or 16-byte vectors");
     if constexpr (V * sizeof(S) == 16) {
         const uint4 r = __ldg(reinterpret_cast<const uint4 *>(p));
         memcpy(out, &r, 16);
-    } else {
+    } else if constexpr (V * sizeof(S) == 8) {
         const uint2 r = __ldg(reinterpret_cast<const uint2 *>(p));
         memcpy(out, &r, 8);
+    } else {
+        const unsigned r = __ldg(reinterpret_cast<const unsigned *>(p));
+        memcpy(out, &r, 4);
     }
 }
 template <class S, int V>
