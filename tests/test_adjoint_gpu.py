@@ -124,3 +124,27 @@ def test_autograd_harness(capi):
     assert abs(float(J.detach()) - J2) <= 1e-15 * abs(J2)
     np.testing.assert_allclose(lid.grad.numpy(), g_lid, rtol=1e-12, atol=0)
     assert abs(float(tau.grad) - g_tau) <= 1e-12 * abs(g_tau)
+
+
+@pytest.mark.parametrize("prec,dim,iters", [("fp64", 12, 15), ("fp64", 16, 20), ("fp32", 16, 20)])
+def test_adjoint_matches_reference_adjoint(capi, prec, dim, iters):
+    """Field by field against the independent numpy FP64 adjoint of the
+    reference algorithm (oracle/adjoint_ref.py)."""
+    from oracle import adjoint_ref
+    rng = np.random.default_rng(dim + iters)
+    lid = 0.05 + 0.01 * rng.standard_normal(dim * dim)
+    target = 0.02 * rng.standard_normal(dim * dim)
+    tau, plane = 0.55, dim // 2
+    J_ref, gt_ref, gl_ref, a0_ref = adjoint_ref.run(dim, None, lid, tau, iters, plane, target)
+    with capi.Lattice(dim, velocity=0.0, precision=prec, lid=lid, tau=tau, stride=0) as L:
+        L.adjoint_set_loss(plane, target)
+        J = L.adjoint_forward(iters, 4)
+        gt, gl, g0 = L.adjoint_backward(1.0)
+    g0 = g0.reshape(19, dim, dim, dim).astype(np.float64)
+    tol = 1e-10 if prec == "fp64" else 2e-4
+    assert abs(J - J_ref) <= tol * J_ref
+    scale = np.abs(a0_ref).max()
+    bad = np.argwhere(np.abs(g0 - a0_ref) > tol * scale)
+    assert bad.size == 0, f"{len(bad)} slots differ, first (q, z, y, x) = {bad[:5].tolist()}"
+    assert np.abs(gl - gl_ref).max() <= tol * np.abs(gl_ref).max()
+    assert abs(gt - gt_ref) <= tol * abs(gt_ref)
