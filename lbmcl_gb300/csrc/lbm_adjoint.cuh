@@ -139,13 +139,11 @@ __device__ __forceinline__ void adjoint_fluid_pairs(const A (&g)[Q], A (&b)[Q], 
     A Gx[3] = {0, 0, 0}, Gy[3] = {0, 0, 0}, Gz[3] = {0, 0, 0};
     // (i, i') pairs with e_i listed first
     constexpr int P[9][2] = {{1, 3}, {2, 4}, {6, 5}, {7, 9}, {8, 10}, {11, 17}, {12, 18}, {15, 13}, {16, 14}};
-    A av[9];
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
         const int i = P[k][0], j = P[k][1];
         const int c = wclass_of(i);
         const A aa = (A)ex_of(i) * ux + (A)ey_of(i) * uy + (A)ez_of(i) * uz;
-        av[k] = aa;
         const A sm = b[i] + b[j], df = b[i] - b[j];
         B[c] += sm * (c0 + (A)4.5 * aa * aa) + (A)3 * aa * df;
         SB[c] += sm;
@@ -154,7 +152,8 @@ __device__ __forceinline__ void adjoint_fluid_pairs(const A (&g)[Q], A (&b)[Q], 
         if (ey_of(i)) Gy[c] += ey_of(i) > 0 ? q : -q;
         if (ez_of(i)) Gz[c] += ez_of(i) > 0 ? q : -q;
     }
-    const A w0 = w_of<A>(0), w1 = w_of<A>(1), w2 = w_of<A>(2);
+    // class weights: rest, axis (population 1), edge (population 7)
+    const A w0 = w_of<A>(0), w1 = w_of<A>(1), w2 = w_of<A>(7);
     const A B0 = w0 * B[0] + w1 * B[1] + w2 * B[2];
     const A sb = w0 * SB[0] + w1 * SB[1] + w2 * SB[2];
     const A gx = w1 * Gx[1] + w2 * Gx[2] - (A)3 * ux * sb;
