@@ -171,7 +171,8 @@ int lbm_adjoint_set_loss(lbm_t *h, int plane_y, const double *target_ux);
 /* Run `iterations` iterations from the current state (as lbm_step without
  * macro output), keeping a checkpoint of the state every `checkpoint_every`
  * iterations (1 = the whole trajectory), and return the loss of the final
- * state.  Synchronous. */
+ * state.  Device memory: ceil(iterations / checkpoint_every) states here,
+ * checkpoint_every - 1 more on the first lbm_adjoint_backward.  Synchronous. */
 int lbm_adjoint_forward(lbm_t *h, int iterations, int checkpoint_every, double *loss);
 
 /* Backward sweep of the last lbm_adjoint_forward, scaled by dloss (dL/dJ for

@@ -240,12 +240,6 @@ int lbm_adjoint_forward(lbm_t *h, int iterations, int checkpoint_every, double *
         if (rc != LBM_OK) return rc;
         s.ckpt.push_back(p);
     }
-    for (int k = 0; k < c - 1; ++k) {
-        void *p = nullptr;
-        int rc = alloc_tracked(h, &p, fbytes);
-        if (rc != LBM_OK) return rc;
-        s.seg.push_back(p);
-    }
     s.iterations = iterations;
     s.every = c;
     s.init_state = h->state_is_init;
@@ -333,8 +327,17 @@ int lbm_adjoint_backward(lbm_t *h, double dloss, double *grad_tau, double *grad_
     a.dloss = m > 0 ? dloss * 2.0 / m : 0.0;
     ADJ_CUDA(loss_seed(h, a));
 
-    // segments, last to first
+    // segment states (c - 1), allocated on the first backward sweep only, so
+    // a loss-only forward holds just its checkpoints
     const int T = s.iterations, c = s.every;
+    const size_t fbytes = (size_t)lbm::Q * h->n * lbm::storage_bytes(h->prec);
+    while ((int)s.seg.size() < c - 1) {
+        void *p = nullptr;
+        int rc = alloc_tracked(h, &p, fbytes);
+        if (rc != LBM_OK) return rc;
+        s.seg.push_back(p);
+    }
+    // segments, last to first
     const int nck = (T + c - 1) / c;
     for (int j = nck - 1; j >= 0; --j) {
         const int start = j * c, end = std::min(T, start + c);
