@@ -3,7 +3,8 @@
 // Same flags, defaults, validation messages and exit codes as the reference
 // (lbm_options.hpp:32-196 of LBMCL): -P -D -d -n -u -i -e -v -w -s -F -o -p
 // -m -f -h.  Long-only additions for this implementation: --precision
-// (fp32|fp64|fp16|bf16), --seed, --noise, --kernel (auto|direct|narrow|staged).
+// (fp32|fp64|fp16|bf16), --seed, --noise, --kernel (auto|direct|narrow|staged),
+// --format (ascii|binary: VTI with raw appended data and f_<it>.raw dumps).
 #pragma once
 
 #include <getopt.h>
@@ -40,6 +41,7 @@ struct lbm_options {
     unsigned long long seed = 0;
     double noise = 0.0;
     int kernel = LBM_KERNEL_AUTO;
+    bool binary = false;  // --format binary
 
     void print_help()
     {
@@ -62,6 +64,7 @@ struct lbm_options {
                      "    --seed N              Seed of the initial noise                      \n"
                      "    --noise S             Std-dev of N(0,S^2) noise on FLUID populations \n"
                      "    --kernel K            Iteration kernel: auto direct narrow staged    \n"
+                     "    --format F            Output files: ascii (default) or binary        \n"
                      "-h  --help                Show this help message and exit                \n";
         exit(1);
     }
@@ -79,7 +82,7 @@ struct lbm_options {
     {
         opterr = 0;
         const char *const short_opts = "P:D:d:n:u:i:e:v:w:s:Fop:mfh";
-        enum { OPT_PRECISION = 1000, OPT_SEED, OPT_NOISE, OPT_KERNEL };
+        enum { OPT_PRECISION = 1000, OPT_SEED, OPT_NOISE, OPT_KERNEL, OPT_FORMAT };
         const option long_opts[] = {
             {"platform", required_argument, nullptr, 'P'},
             {"device", required_argument, nullptr, 'D'},
@@ -101,6 +104,7 @@ struct lbm_options {
             {"seed", required_argument, nullptr, OPT_SEED},
             {"noise", required_argument, nullptr, OPT_NOISE},
             {"kernel", required_argument, nullptr, OPT_KERNEL},
+            {"format", required_argument, nullptr, OPT_FORMAT},
             {nullptr, no_argument, nullptr, 0},
         };
 
@@ -186,6 +190,13 @@ struct lbm_options {
                 else if (k == "narrow") kernel = LBM_KERNEL_NARROW;
                 else if (k == "staged") kernel = LBM_KERNEL_STAGED;
                 else { std::cerr << "Please enter a valid kernel (auto direct narrow staged)" << std::endl; exit(1); }
+                break;
+            }
+            case OPT_FORMAT: {
+                const std::string f = optarg;
+                if (f == "ascii") binary = false;
+                else if (f == "binary") binary = true;
+                else { std::cerr << "Please enter a valid format (ascii binary)" << std::endl; exit(1); }
                 break;
             }
             case 'h':

@@ -77,6 +77,7 @@ class LBMCL
     unsigned long long seed = 0;
     double noise = 0.0;
     int kernel = LBM_KERNEL_AUTO;
+    bool binary = false;  // raw appended VTI and f_<it>.raw dumps
     int device = 0;
 
     lbm_t *h = nullptr;
@@ -136,7 +137,14 @@ class LBMCL
         check(lbm_dump(h, LBM_DUMP_F, f.data(), f.size() * sizeof(T)));
         std::ostringstream name;
         name << dump_path << "/f_" << std::setw((int)lbmcl::digits(iterations)) << std::setfill('0') << iteration
-             << ".dump";
+             << (binary ? ".raw" : ".dump");
+        if (binary) {
+            // the f buffer as the device holds it in the reference's layout:
+            // 19 * dim^3 little-endian values in the CSoA order of `stride`
+            std::ofstream raw(name.str(), std::ios::binary);
+            raw.write(reinterpret_cast<const char *>(f.data()), (std::streamsize)(f.size() * sizeof(T)));
+            return;
+        }
         std::ofstream out(name.str());
         const size_t dd = lbmcl::digits(dim);
         const size_t coord_spaces = dd * 3 + 5;
@@ -169,8 +177,49 @@ class LBMCL
         out << '\n';
     }
 
+    // lbmcl.<it>.vti with raw appended data: the same ImageData, extent and
+    // arrays as the ASCII file; each array is a UInt64 byte count followed by
+    // its values (rho, then v with the three components interleaved)
+    void storeDataBinary(const std::string &path, const std::vector<T> &rho, const std::vector<T> &u)
+    {
+        const size_t n = n_sites();
+        const size_t from = 1, to = dim - 1, extent = to - from - 1, m = dim - 2;
+        const size_t npts = m * m * m;
+        std::vector<T> r(npts), v(3 * npts);
+        size_t k = 0;
+        for (size_t z = from; z < to; ++z)
+            for (size_t y = from; y < to; ++y)
+                for (size_t x = from; x < to; ++x, ++k) {
+                    const size_t id = x + y * dim + z * dim * dim;
+                    r[k] = rho[id];
+                    for (size_t c = 0; c < 3; ++c) v[3 * k + c] = u[c * n + id];
+                }
+        const uint64_t rb = npts * sizeof(T), vb = 3 * npts * sizeof(T);
+        const char *type = std::is_same<T, float>::value ? "Float32" : "Float64";
+        std::ofstream out(path, std::ios::binary);
+        out << "<?xml version=\"1.0\"?>\n"
+            << "<VTKFile type=\"ImageData\" version=\"0.1\" byte_order=\"LittleEndian\" header_type=\"UInt64\">\n"
+            << "  <ImageData WholeExtent=\"0 " << extent << " 0 " << extent << " 0 " << extent
+            << "\" Origin=\"0 0 0\" Spacing=\"1 1 1\">\n"
+            << "    <Piece Extent=\"0 " << extent << " 0 " << extent << " 0 " << extent << "\">\n"
+            << "      <PointData Scalars=\"rho\">\n"
+            << "        <DataArray type=\"" << type
+            << "\" Name=\"rho\" NumberOfComponents=\"1\" format=\"appended\" offset=\"0\"/>\n"
+            << "        <DataArray type=\"" << type << "\" Name=\"v\" NumberOfComponents=\"3\" format=\"appended\" offset=\""
+            << (sizeof(uint64_t) + rb) << "\"/>\n"
+            << "      </PointData>\n"
+            << "    </Piece>\n"
+            << "  </ImageData>\n"
+            << "  <AppendedData encoding=\"raw\">\n   _";
+        out.write(reinterpret_cast<const char *>(&rb), sizeof rb);
+        out.write(reinterpret_cast<const char *>(r.data()), (std::streamsize)rb);
+        out.write(reinterpret_cast<const char *>(&vb), sizeof vb);
+        out.write(reinterpret_cast<const char *>(v.data()), (std::streamsize)vb);
+        out << "\n  </AppendedData>\n</VTKFile>\n";
+    }
+
     // lbmcl.<it>.vti, ASCII ImageData of the interior [1, dim-2]^3
-    // (lbmcl.hpp:261-334)
+    // (lbmcl.hpp:261-334); --format binary writes raw appended data instead
     void storeData(size_t iteration)
     {
         const size_t n = n_sites();
@@ -180,6 +229,10 @@ class LBMCL
         std::ostringstream name;
         name << vtk_path << "/lbmcl." << std::setw((int)lbmcl::digits(iterations)) << std::setfill('0') << iteration
              << ".vti";
+        if (binary) {
+            storeDataBinary(name.str(), rho, u);
+            return;
+        }
         std::ofstream out(name.str());
         const size_t from = 1, to = dim - 1, extent = to - from - 1;
         const char *type = std::is_same<T, float>::value ? "Float32" : "Float64";
@@ -259,6 +312,7 @@ public:
 
     void setNoise(unsigned long long s, double sigma) { seed = s; noise = sigma; }
     void setKernel(int k) { kernel = k; }
+    void setBinary(bool b) { binary = b; }
 
     // lbmcl.hpp:392-482 + the initialize enqueue (lbmcl.hpp:494-498): one
     // handle owns every buffer; lbm_init also runs the initialisation kernel.
@@ -362,7 +416,8 @@ public:
                   << "every            = " << every << "\n"
                   << "VTK PATH         = " << vtk_path << "\n"
                   << "DUMP F           = " << dump_f << "\n"
-                  << "DUMP MAP         = " << dump_map << "\n";
+                  << "DUMP MAP         = " << dump_map << "\n"
+                  << "FORMAT           = " << (binary ? "binary" : "ascii") << "\n";
     }
 
     // lbmcl.hpp:648-669: the ';'-separated line benchmark.sh aggregates

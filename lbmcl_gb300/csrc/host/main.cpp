@@ -14,6 +14,7 @@ void performSimulation(const lbm_options &opts)
                    opts.dump_f, opts.lws_given, opts.precision());
     lbmcl.setNoise(opts.seed, opts.noise);
     lbmcl.setKernel(opts.kernel);
+    lbmcl.setBinary(opts.binary);
     lbmcl.setupSimulation(opts.platformID, opts.deviceID);
     lbmcl.printConfiguration();
     lbmcl.performSimulation();

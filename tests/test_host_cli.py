@@ -156,3 +156,72 @@ def test_double_and_sixteen_bit_runs(lbmcl_bin, oracle, tmp_path, capi):
         assert r.returncode == 0, r.stderr
         got = vti.read_vti(str(d / "lbmcl.40.vti"))
         assert np.isfinite(np.nan_to_num(got["rho"], nan=1.0)).all()
+
+
+# --------------------------------------------------------- binary output ------
+def test_binary_vti_round_trip_cpu(tmp_path):
+    """write_vti_binary (raw and zlib) reads back to the same arrays as the
+    ASCII file of the same fields."""
+    from lbmcl_gb300 import vti
+    rng = np.random.default_rng(3)
+    dim = 10
+    for dt in (np.float32, np.float64):
+        rho = rng.standard_normal(dim ** 3).astype(dt)
+        u = rng.standard_normal(3 * dim ** 3).astype(dt)
+        rho[0] = np.nan  # a wall site: outside the interior, never written
+        want = vti.interior_fields(dim, rho, u)
+        vti.write_vti_ascii(str(tmp_path / "a.vti"), dim, rho, u)
+        a = vti.read_vti(str(tmp_path / "a.vti"))
+        for comp in (False, True):
+            p = tmp_path / f"b{int(comp)}.vti"
+            vti.write_vti_binary(str(p), dim, rho, u, compress=comp, block=1000)
+            b = vti.read_vti(str(p))
+            assert b["extent"] == a["extent"] == (0, dim - 3, 0, dim - 3, 0, dim - 3)
+            for name in ("rho", "v"):
+                assert b[name].dtype == dt
+                np.testing.assert_array_equal(b[name], want[name])
+                np.testing.assert_array_equal(b[name], a[name])
+
+
+def test_read_f_raw_de_indexes_csoa_cpu(tmp_path, oracle):
+    from lbmcl_gb300 import vti
+    dim, n = 8, 512
+    f = np.arange(19 * n, dtype=np.float32).reshape(19, n)
+    for stride in (1, 8, 64, n):
+        buf = oracle.soa_to_csoa(f.reshape(19, dim, dim, dim), dim, stride)
+        buf.astype(np.float32).tofile(tmp_path / "f.raw")
+        np.testing.assert_array_equal(vti.read_f_raw(str(tmp_path / "f.raw"), dim, stride), f)
+
+
+def test_rejects_bad_format(lbmcl_bin):
+    r = run(lbmcl_bin, "--format", "hdf5")
+    assert r.returncode == 1 and "Please enter a valid format" in r.stderr
+
+
+@pytest.mark.gpu
+def test_binary_format_matches_oracle(lbmcl_bin, oracle, tmp_path, capi):
+    """--format binary at 8^3 (-f, every iteration): the raw appended VTI holds
+    the oracle's rho, u bit for bit, f_<it>.raw the oracle's f buffer in the
+    CSoA layout of the run's stride."""
+    from lbmcl_gb300 import vti
+    for prec, dt, flag in (("f32", np.float32, []), ("f64", np.float64, ["-F"])):
+        d = tmp_path / prec
+        d.mkdir()
+        r = run(lbmcl_bin, "-d", 8, "-i", 4, "-e", 1, "-s", 8, "-v", d, "-p", d, "-f", "--format", "binary", *flag)
+        assert r.returncode == 0, r.stderr
+        assert "FORMAT           = binary" in r.stdout
+        o = oracle.OracleLattice(8, 0.0089, 0.05, prec, 8)
+        for it in range(0, 5):
+            if it:
+                o.step(1, every=1)
+            got = vti.read_vti(str(d / f"lbmcl.{it}.vti"))
+            want = vti.interior_fields(8, o.rho, o.u)
+            for name in ("rho", "v"):
+                assert got[name].dtype == dt
+                np.testing.assert_array_equal(got[name], want[name])
+        o = oracle.OracleLattice(8, 0.0089, 0.05, prec, 8)
+        for it in range(0, 5):
+            if it >= 2:  # f_<it> is the buffer iteration it reads: f_0 and f_1 both hold the init state
+                o.step(1)
+            raw = np.fromfile(d / f"f_{it}.raw", dt)
+            np.testing.assert_array_equal(np.nan_to_num(raw, nan=-7.0), np.nan_to_num(o.state, nan=-7.0))
