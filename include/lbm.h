@@ -92,6 +92,8 @@ typedef struct lbm_config {
     int kernel;                /* lbm_kernel: iteration kernel variant; 0 = the tuned default
                                   (NARROW for FP32, DIRECT otherwise)                       */
     int stages;                /* TMA-staged kernel: pipeline depth (0 = tuned default)    */
+    int adjoint_steps;         /* adjoint steps per launch of the backward sweep: 0 = tuned
+                                  default (2 for the FP32 adjoint, 1 for FP64), 1, or 2     */
 } lbm_config;
 
 /* Iteration kernel variants (same results, different data movement). */

@@ -47,6 +47,7 @@ class Config(C.Structure):
         ("profile_steps", C.c_int),
         ("kernel", C.c_int),
         ("stages", C.c_int),
+        ("adjoint_steps", C.c_int),
     ]
 
 
@@ -115,12 +116,13 @@ class Lattice:
 
     precision: "fp32" | "fp64" | "fp16" | "bf16".  stride: CSoA stride of F
     dumps (None = dim^3).  lid: optional per-column lid u_x, shape (dim, dim)
-    indexed [y, x] or flat x + y*dim.
+    indexed [y, x] or flat x + y*dim.  adjoint_steps: adjoint steps per
+    launch of the backward sweep (0 = default, 1, 2).
     """
 
     def __init__(self, dim, viscosity=0.0089, velocity=0.05, precision="fp32", stride=None, lid=None,
                  seed=0, noise_sigma=0.0, tau=0.0, block_threads=0, max_device_bytes=0, device=0,
-                 profile_steps=False, kernel=0, stages=0):
+                 profile_steps=False, kernel=0, stages=0, adjoint_steps=0):
         L = lib()
         c = default_config()
         c.dim = int(dim)
@@ -141,6 +143,7 @@ class Lattice:
         c.profile_steps = 1 if profile_steps else 0
         c.kernel = KERNELS[kernel] if isinstance(kernel, str) else int(kernel)
         c.stages = int(stages)
+        c.adjoint_steps = int(adjoint_steps)
         self.cfg = c
         self.dim = int(dim)
         self.n = self.dim ** 3

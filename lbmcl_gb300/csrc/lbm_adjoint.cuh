@@ -326,6 +326,201 @@ __global__ void __launch_bounds__(256, adj_min_blocks<S>()) adjoint_kernel(AdjAr
     block_reduce_add((double)dw, a.tau_acc + a.tau_base);
 }
 
+// ---------------------------------------------------------------------------
+// Two adjoint steps per launch, a_{k+1} -> a_k -> a_{k-1}, for the FP32
+// adjoint (forward storage FP32, FP16 or BF16).
+//
+// A block owns a tile of ADJ2_TX x ADJ2_TY columns of [1, dim-2]^2 and a chunk
+// of z-planes, and marches the chunk in z.  Step A computes a_k, one thread
+// per site, on the tile plus a one-site ring in x and y (the ext tile,
+// ADJ2_EX x ADJ2_EY = the block), plane by plane, into shared memory; step B,
+// one plane behind, computes a_{k-1} on the tile from the shared a_k and
+// writes it.  a_k never reaches global memory, so a pair of steps moves
+// a_{k+1} in, Q_k and Q_{k-1} in, a_{k-1} out: 2 x 76 + 2 x 19 x sizeof(S)
+// bytes per site instead of twice 2 x 76 + 19 x sizeof(S).
+//
+// Step B at plane q reads population i of a_k at plane q + ez_i, x + ex_i,
+// y + ey_i.  Populations 0, 5 and 6 have no x, y offset: the same thread
+// computed them, so they stay in registers (pop 6 of this plane, pop 0 of the
+// last, pop 5 of the one before).  The other 16 live in shared memory for
+// the planes still to be read; with one barrier per plane the writer of plane
+// p+1 runs alongside the readers of plane p-1, so a population needs 2, 3 or
+// 4 plane slots for ez_i = +1, 0, -1 (48 slots, 49,152 bytes).  Three blocks
+// per SM at 80 registers measured faster than four at 64 (which spills).
+// Sums for tau and the lid gradient count a site once: step A's
+// contributions only on the block's own tile and planes.
+//
+// Element offsets are 32-bit (i * n + site < 2^32: 19 dim^3 < 2^32, dim <=
+// 609); larger lattices take the one-step kernels.
+// ---------------------------------------------------------------------------
+constexpr int ADJ2_EX = 32, ADJ2_EY = 8;                    // block = ext tile
+constexpr int ADJ2_TX = ADJ2_EX - 2, ADJ2_TY = ADJ2_EY - 2;  // owned tile
+__host__ __device__ constexpr bool adj2_in_regs(int i) { return i == 0 || i == 5 || i == 6; }
+__host__ __device__ constexpr int adj2_depth(int i)
+{
+    return adj2_in_regs(i) ? 0 : (ez_of(i) == 1 ? 2 : (ez_of(i) == 0 ? 3 : 4));
+}
+// first plane slot of each population; used through a constexpr local, so
+// that every index is an immediate (a call at run time would recurse)
+struct Adj2Layout {
+    int base[Q + 1];
+};
+__host__ __device__ constexpr Adj2Layout adj2_layout()
+{
+    Adj2Layout l{};
+    for (int i = 0; i < Q; ++i) l.base[i + 1] = l.base[i] + adj2_depth(i);
+    return l;
+}
+constexpr int ADJ2_SLOTS = adj2_layout().base[Q];
+constexpr size_t ADJ2_SMEM = (size_t)ADJ2_SLOTS * ADJ2_EX * ADJ2_EY * sizeof(float);
+static_assert(ADJ2_SLOTS == 48, "plane slots of the two-step adjoint");
+// the largest dim whose 19 dim^3 element offsets fit 32 bits
+constexpr int ADJ2_MAX_DIM = 609;
+
+struct Adj2Args {
+    const void *fwd_a;   // Q_k, forward state of step A
+    const void *fwd_b;   // Q_{k-1}, forward state of step B
+    const float *ain;    // a_{k+1}
+    float *aout;         // a_{k-1}
+    const uint8_t *map;
+    const void *lid;     // forward macro type, dim*dim
+    double *grad_lid;    // dim*dim
+    double *tau_acc;     // per block
+    unsigned n;          // dim^3
+    int dim;
+    int ntx, nty;        // tiles in x and y
+    int zc;              // planes per chunk
+    float omega;
+    // per-population element offsets from a site (mod 2^32): i n + e_i
+    // (reverse streaming), i n - e_i (forward pull), i n (own slot); kernel
+    // parameters, so the unrolled loops take them as constant operands
+    unsigned off_up[Q], off_down[Q], off_own[Q];
+};
+
+#ifndef LBM_ADJ2_MINB
+#define LBM_ADJ2_MINB 3
+#endif
+
+// a_k(s) of one site of step A or B: b = the reverse-streamed adjoint,
+// fwd = Q of the step; d, l = its tau and lid terms.
+template <class S>
+__device__ __forceinline__ void adjoint_site(const S *__restrict__ fwd, const unsigned (&off)[Q], unsigned site,
+                                             uint8_t b8, float lidv, float omega, const Weights<float> &W,
+                                             float (&b)[Q], float &d, float &l)
+{
+    float g[Q];
+#pragma unroll
+    for (int i = 0; i < Q; ++i) g[i] = fwd_value<S, float>(load_one(fwd + (site + off[i])), i);
+    if (b8 == 0) adjoint_fluid_pairs<float>(g, b, omega, d);
+    else adjoint_general<float, float>(g, b, b8, lidv, omega, W, d, l);
+}
+
+template <class S>
+__global__ void __launch_bounds__(ADJ2_EX * ADJ2_EY, LBM_ADJ2_MINB) adjoint2_kernel(Adj2Args a)
+{
+    extern __shared__ float adj2_smem[];  // [ADJ2_SLOTS][ADJ2_EY][ADJ2_EX]
+    constexpr int PL = ADJ2_EX * ADJ2_EY;
+    constexpr Adj2Layout LAY = adj2_layout();
+    const int dim = a.dim;
+    const unsigned plane = (unsigned)dim * (unsigned)dim;
+    const int lx = (int)threadIdx.x % ADJ2_EX, ly = (int)threadIdx.x / ADJ2_EX;
+    int t = (int)blockIdx.x;
+    const int tx = t % a.ntx;
+    t /= a.ntx;
+    const int ty = t % a.nty, tz = t / a.nty;
+    const int xi0 = 1 + tx * ADJ2_TX, yi0 = 1 + ty * ADJ2_TY, zi0 = 1 + tz * a.zc;
+    const int zi1 = min(zi0 + a.zc, dim - 1);  // owned planes [zi0, zi1)
+    const int x = xi0 - 1 + lx, y = yi0 - 1 + ly;
+    const bool in_dom = x < dim && y < dim;
+    const bool owned = lx >= 1 && lx <= ADJ2_TX && ly >= 1 && ly <= ADJ2_TY && x <= dim - 2 && y <= dim - 2;
+    // block-uniform: every site of the ext tile / owned tile in x, y is FLUID
+    // on the planes [2, dim-3]
+    const bool ext_fluid = xi0 - 1 >= 2 && xi0 + ADJ2_EX - 2 <= dim - 3 && yi0 - 1 >= 2 && yi0 + ADJ2_EY - 2 <= dim - 3;
+    const bool own_fluid = xi0 >= 2 && xi0 + ADJ2_TX - 1 <= dim - 3 && yi0 >= 2 && yi0 + ADJ2_TY - 1 <= dim - 3;
+    const S *fwd_a = static_cast<const S *>(a.fwd_a);
+    const S *fwd_b = static_cast<const S *>(a.fwd_b);
+    const float *lid = static_cast<const float *>(a.lid);
+    const Weights<float> W = make_weights<float>();
+    const float omega = a.omega;
+    float dw = 0.f, dl = 0.f;
+    const unsigned col = (unsigned)y * (unsigned)dim + (unsigned)x;
+    // register-held populations of a_k: pop 0 of plane p-1, pop 5 of planes
+    // p-1 and p-2 (as of step B of plane p-1)
+    float r0_prev = 0.f, r5_prev1 = 0.f, r5_prev2 = 0.f;
+
+    for (int p = zi0 - 1; p <= zi1; ++p) {
+        float r0, r5, r6;
+        // ---- step A: a_k at (x, y, p) of the ext tile
+        {
+            float b[Q];
+            const unsigned site = (unsigned)p * plane + col;
+            uint8_t b8 = M_WALL;
+            if (in_dom) b8 = (ext_fluid && p >= 2 && p <= dim - 3) ? (uint8_t)0 : __ldg(a.map + site);
+            if (b8 & M_WALL) {
+#pragma unroll
+                for (int i = 0; i < Q; ++i) b[i] = 0.f;
+            } else {
+#pragma unroll
+                for (int i = 0; i < Q; ++i) b[i] = __ldg(a.ain + (site + a.off_up[i]));
+                float d = 0.f, l = 0.f;
+                const float lidv = (b8 & M_FRONT) ? lid[col] : 0.f;
+                adjoint_site<S>(fwd_a, a.off_down, site, b8, lidv, omega, W, b, d, l);
+                if (owned && p >= zi0 && p < zi1) {
+                    dw += d;
+                    dl += l;
+                }
+            }
+            const int m2 = p & 1, m3 = p % 3, m4 = p & 3;
+#pragma unroll
+            for (int i = 0; i < Q; ++i) {
+                if (adj2_in_regs(i)) continue;
+                const int slot = LAY.base[i] + (adj2_depth(i) == 2 ? m2 : (adj2_depth(i) == 3 ? m3 : m4));
+                adj2_smem[slot * PL + threadIdx.x] = b[i];
+            }
+            r0 = b[0];
+            r5 = b[5];
+            r6 = b[6];
+        }
+        __syncthreads();
+        // ---- step B: a_{k-1} at (x, y, p - 1) of the owned tile
+        const int q = p - 1;
+        if (owned && q >= zi0) {
+            const unsigned site = (unsigned)q * plane + col;
+            const uint8_t b8 = (own_fluid && q >= 2 && q <= dim - 3) ? (uint8_t)0 : __ldg(a.map + site);
+            // plane q + ez_i of population i: p (ez = +1), p - 1 (0), p - 2 (-1)
+            const int m2 = p & 1, m3 = (p + 2) % 3, m4 = (p + 2) & 3;
+            float b[Q];
+#pragma unroll
+            for (int i = 0; i < Q; ++i) {
+                if (adj2_in_regs(i)) continue;
+                const int slot = LAY.base[i] + (adj2_depth(i) == 2 ? m2 : (adj2_depth(i) == 3 ? m3 : m4));
+                b[i] = adj2_smem[slot * PL + (ly + ey_of(i)) * ADJ2_EX + (lx + ex_of(i))];
+            }
+            b[0] = r0_prev;
+            b[5] = r5_prev2;
+            b[6] = r6;
+            if (b8 & M_WALL) {
+#pragma unroll
+                for (int i = 0; i < Q; ++i) b[i] = 0.f;
+            } else {
+                float d = 0.f, l = 0.f;
+                const float lidv = (b8 & M_FRONT) ? lid[col] : 0.f;
+                adjoint_site<S>(fwd_b, a.off_down, site, b8, lidv, omega, W, b, d, l);
+                dw += d;
+                dl += l;
+            }
+#pragma unroll
+            for (int i = 0; i < Q; ++i) a.aout[site + a.off_own[i]] = b[i];
+        }
+        r0_prev = r0;
+        r5_prev2 = r5_prev1;
+        r5_prev1 = r5;
+    }
+    // one MOVING site per column, in one chunk: a single writer per column
+    if (owned && zi0 <= dim - 2 && dim - 2 < zi1) a.grad_lid[col] += (double)dl;
+    block_reduce_add((double)dw, a.tau_acc);
+}
+
 // Seed of the backward sweep: a_T = dJ/dR_T for the mid-plane loss
 //   J = (1/M) sum over the FLUID sites of plane y = plane_y of (u_x - target)^2,
 // dJ/dR_T(s, i) = (2/M) (u_x - target) (e_ix - u_x) / rho; zero elsewhere.

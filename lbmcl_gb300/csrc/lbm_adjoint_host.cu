@@ -8,7 +8,8 @@
 // a_T = dJ/dR_T, then walks the segments backwards: it restores a
 // checkpoint, recomputes the segment's intermediate states with the forward
 // kernel, and applies the adjoint step from the segment's last iteration to
-// its first.  Memory: ceil(T/c) checkpoints + (c - 1) segment states, i.e.
+// its first, two steps per launch for the FP32 adjoint (a segment of odd
+// length ends with one single step).  Memory: ceil(T/c) checkpoints + (c - 1) segment states, i.e.
 // about 2 sqrt(T) states for c = sqrt(T); one extra forward iteration per
 // iteration of the backward sweep.
 #include <algorithm>
@@ -106,6 +107,69 @@ cudaError_t run_lid_init_grad(const lbm::AdjArgs &a, cudaStream_t s)
     const int nc = a.dim * a.dim;
     lbm::lid_init_grad_kernel<S><<<(nc + 255) / 256, 256, 0, s>>>(a);
     return cudaGetLastError();
+}
+
+// ---- two steps per launch (FP32 adjoint)
+constexpr int kAdj2Chunk = 32;  // z-planes per block
+
+bool two_step(const lbm_t *h)
+{
+    return h->prec != LBM_FP64 && h->cfg.adjoint_steps != 1 && h->dim <= lbm::ADJ2_MAX_DIM;
+}
+
+unsigned adj2_grid(const lbm_t *h, int &ntx, int &nty)
+{
+    const int m = h->dim - 2;
+    ntx = (m + lbm::ADJ2_TX - 1) / lbm::ADJ2_TX;
+    nty = (m + lbm::ADJ2_TY - 1) / lbm::ADJ2_TY;
+    const int ntz = (m + kAdj2Chunk - 1) / kAdj2Chunk;
+    return (unsigned)ntx * (unsigned)nty * (unsigned)ntz;
+}
+
+template <class S>
+cudaError_t run_adjoint2(const lbm::Adj2Args &a, unsigned grid, cudaStream_t s)
+{
+    static bool attr = false;  // per process: the attribute is per function, not per device
+    if (!attr) {
+        const cudaError_t e = cudaFuncSetAttribute(lbm::adjoint2_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                   (int)lbm::ADJ2_SMEM);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    lbm::adjoint2_kernel<S><<<grid, lbm::ADJ2_EX * lbm::ADJ2_EY, lbm::ADJ2_SMEM, s>>>(a);
+    return cudaGetLastError();
+}
+
+// a_{k+1} -> a_{k-1} with Q_k (fwd_a) and Q_{k-1} (fwd_b)
+cudaError_t adjoint_two_steps(const lbm_t *h, const void *fwd_a, const void *fwd_b, const void *ain, void *aout)
+{
+    lbm::Adj2Args a = {};
+    a.fwd_a = fwd_a;
+    a.fwd_b = fwd_b;
+    a.ain = static_cast<const float *>(ain);
+    a.aout = static_cast<float *>(aout);
+    a.map = h->map;
+    a.lid = h->lid;
+    a.grad_lid = h->adj.grad_lid;
+    a.tau_acc = h->adj.tau_acc;
+    a.n = (unsigned)h->n;
+    a.dim = h->dim;
+    a.zc = kAdj2Chunk;
+    for (int i = 0; i < lbm::Q; ++i) {
+        const long long sh = lbm::ex_of(i) + (long long)lbm::ey_of(i) * h->dim +
+                             (long long)lbm::ez_of(i) * h->dim * h->dim;
+        const unsigned long long base = (unsigned long long)i * h->n;
+        a.off_up[i] = (unsigned)(base + (unsigned long long)sh);
+        a.off_down[i] = (unsigned)(base - (unsigned long long)sh);
+        a.off_own[i] = (unsigned)base;
+    }
+    a.omega = (float)h->inv_tau;
+    const unsigned grid = adj2_grid(h, a.ntx, a.nty);
+    switch (h->prec) {
+    case LBM_FP32: return run_adjoint2<float>(a, grid, h->stream);
+    case LBM_FP16: return run_adjoint2<__half>(a, grid, h->stream);
+    default: return run_adjoint2<__nv_bfloat16>(a, grid, h->stream);
+    }
 }
 
 cudaError_t adjoint_step(const lbm_t *h, const lbm::AdjArgs &a)
@@ -295,7 +359,9 @@ int lbm_adjoint_backward(lbm_t *h, double dloss, double *grad_tau, double *grad_
     const size_t nc = (size_t)h->dim * h->dim;
     unsigned gi, gf;
     adj_grids(h, gi, gf);
-    const unsigned agrid = gi + gf;  // tau partial slots of the two launches
+    int ntx, nty;
+    // tau partial slots: the one-step launch pair, or the two-step launch
+    const unsigned agrid = std::max(gi + gf, two_step(h) ? adj2_grid(h, ntx, nty) : 0u);
     if (!s.adj[0]) {
         int rc = alloc_tracked(h, &s.adj[0], abytes);
         if (rc == LBM_OK) rc = alloc_tracked(h, &s.adj[1], abytes);
@@ -345,9 +411,18 @@ int lbm_adjoint_backward(lbm_t *h, double dloss, double *grad_tau, double *grad_
             const void *fin = (k - 1 == start) ? s.ckpt[j] : s.seg[k - 2 - start];
             ADJ_CUDA(lbm::launch_iteration(h, fin, s.seg[k - 1 - start]));
         }
-        for (int k = end - 1; k >= start; --k) {
+        // Q_k of this segment
+        auto state = [&](int k) -> const void * { return k == start ? s.ckpt[j] : s.seg[k - 1 - start]; };
+        int k = end - 1;
+        if (two_step(h)) {
+            for (; k - 1 >= start; k -= 2) {
+                ADJ_CUDA(adjoint_two_steps(h, state(k), state(k - 1), s.adj[cur], s.adj[cur ^ 1]));
+                cur ^= 1;
+            }
+        }
+        for (; k >= start; --k) {
             lbm::AdjArgs b = adj_args(h);
-            b.fwd = (k == start) ? s.ckpt[j] : s.seg[k - 1 - start];
+            b.fwd = state(k);
             b.ain = s.adj[cur];
             b.aout = s.adj[cur ^ 1];
             ADJ_CUDA(adjoint_step(h, b));

@@ -318,6 +318,8 @@ int lbm_init(lbm_t **out, const lbm_config *c)
     if (c->kernel < LBM_KERNEL_AUTO || c->kernel > LBM_KERNEL_NARROW)
         return fail(LBM_EINVAL, "lbm_init: unknown kernel variant %d", c->kernel);
     if (c->stages < 0 || c->stages > 16) return fail(LBM_EINVAL, "lbm_init: stages %d out of range", c->stages);
+    if (c->adjoint_steps < 0 || c->adjoint_steps > 2)
+        return fail(LBM_EINVAL, "lbm_init: adjoint_steps %d out of range (0, 1, 2)", c->adjoint_steps);
     if (c->block_threads < 0 || c->block_threads > 1024)
         return fail(LBM_EINVAL, "lbm_init: block_threads %d out of range", c->block_threads);
     if (c->lid_profile) {

@@ -76,12 +76,14 @@ def test_initial_population_gradient(capi):
 
 
 def test_checkpointing_is_exact(capi):
-    """Recomputed segments reproduce the stored trajectory bit for bit."""
+    """Recomputed segments reproduce the stored trajectory bit for bit (one
+    adjoint step per launch, so that every schedule sums in the same order)."""
     dim, iters = 24, 50
     lid, target = setup_case(dim, 5)
     out = []
     for every in (1, 8, 50):
-        with capi.Lattice(dim, velocity=0.0, precision="fp32", lid=lid, tau=0.52, seed=1, noise_sigma=1e-4) as L:
+        with capi.Lattice(dim, velocity=0.0, precision="fp32", lid=lid, tau=0.52, seed=1, noise_sigma=1e-4,
+                          adjoint_steps=1) as L:
             L.adjoint_set_loss(12, target)
             L.adjoint_forward(iters, every)
             out.append(L.adjoint_backward(1.0))
@@ -105,6 +107,29 @@ def test_fp32_adjoint_close_to_fp64(capi, prec):
     tol = {"fp32": 1e-4, "fp16": 5e-2, "bf16": 2e-1}[prec]
     assert abs(g[0] - g64[0]) <= tol * abs(g64[0])
     assert np.linalg.norm(g[1] - g64[1]) <= tol * np.linalg.norm(g64[1])
+
+
+@pytest.mark.parametrize("prec", ["fp32", "fp16", "bf16"])
+@pytest.mark.parametrize("dim,iters,every", [(16, 23, 6), (40, 17, 17), (64, 12, 4)])
+def test_two_step_adjoint_matches_one_step(capi, prec, dim, iters, every):
+    """The two-steps-per-launch adjoint (shared-memory a_k) against the
+    one-step kernels: same per-site arithmetic, sums in another order.  dim
+    40 and 64 cross tile and z-chunk borders; odd segment lengths end with a
+    single step."""
+    lid, target = setup_case(dim, dim + iters)
+    res = {}
+    for steps in (1, 2):
+        with capi.Lattice(dim, velocity=0.0, precision=prec, lid=lid, tau=0.53, seed=3, noise_sigma=1e-4,
+                          adjoint_steps=steps) as L:
+            L.adjoint_set_loss(dim // 2, target)
+            J = L.adjoint_forward(iters, every)
+            res[steps] = (J,) + tuple(L.adjoint_backward(1.0))
+    (J1, t1, l1, f1), (J2, t2, l2, f2) = res[1], res[2]
+    assert J1 == J2
+    assert abs(t2 - t1) <= 1e-5 * abs(t1)
+    assert np.abs(l2 - l1).max() <= 1e-5 * np.abs(l1).max()
+    assert np.abs(f2 - f1).max() <= 1e-5 * np.abs(f1).max()
+    assert np.isfinite(f2).all()
 
 
 def test_autograd_harness(capi):

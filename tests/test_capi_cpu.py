@@ -48,6 +48,8 @@ def _init(libonly, **kw):
     (dict(velocity=float("inf")), "velocity"),
     (dict(noise_sigma=-1.0), "noise"),
     (dict(block_threads=4096), "block_threads"),
+    (dict(adjoint_steps=3), "adjoint_steps"),
+    (dict(adjoint_steps=-1), "adjoint_steps"),
 ])
 def test_init_rejects_bad_arguments(libonly, kw, frag):
     rc, msg = _init(libonly, **kw)
