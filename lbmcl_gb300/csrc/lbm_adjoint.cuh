@@ -404,15 +404,19 @@ struct Adj2Args {
 // a_k(s) of one site of step A or B: b = the reverse-streamed adjoint,
 // fwd = Q of the step; d, l = its tau and lid terms.
 template <class S>
-__device__ __forceinline__ void adjoint_site(const S *__restrict__ fwd, const unsigned (&off)[Q], unsigned site,
-                                             uint8_t b8, float lidv, float omega, const Weights<float> &W,
-                                             float (&b)[Q], float &d, float &l)
+__device__ __forceinline__ void adjoint_site(float (&g)[Q], uint8_t b8, float lidv, float omega,
+                                             const Weights<float> &W, float (&b)[Q], float &d, float &l)
 {
-    float g[Q];
-#pragma unroll
-    for (int i = 0; i < Q; ++i) g[i] = fwd_value<S, float>(load_one(fwd + (site + off[i])), i);
     if (b8 == 0) adjoint_fluid_pairs<float>(g, b, omega, d);
     else adjoint_general<float, float>(g, b, b8, lidv, omega, W, d, l);
+}
+// the forward pull R(s) of a site from its step's Q
+template <class S>
+__device__ __forceinline__ void adjoint_pull(const S *__restrict__ fwd, const unsigned (&off)[Q], unsigned site,
+                                             float (&g)[Q])
+{
+#pragma unroll
+    for (int i = 0; i < Q; ++i) g[i] = fwd_value<S, float>(load_one(fwd + (site + off[i])), i);
 }
 
 template <class S>
@@ -462,9 +466,11 @@ __global__ void __launch_bounds__(ADJ2_EX * ADJ2_EY, LBM_ADJ2_MINB) adjoint2_ker
             } else {
 #pragma unroll
                 for (int i = 0; i < Q; ++i) b[i] = __ldg(a.ain + (site + a.off_up[i]));
+                float g[Q];
+                adjoint_pull<S>(fwd_a, a.off_down, site, g);
                 float d = 0.f, l = 0.f;
                 const float lidv = (b8 & M_FRONT) ? lid[col] : 0.f;
-                adjoint_site<S>(fwd_a, a.off_down, site, b8, lidv, omega, W, b, d, l);
+                adjoint_site<S>(g, b8, lidv, omega, W, b, d, l);
                 if (owned && p >= zi0 && p < zi1) {
                     dw += d;
                     dl += l;
@@ -481,12 +487,22 @@ __global__ void __launch_bounds__(ADJ2_EX * ADJ2_EY, LBM_ADJ2_MINB) adjoint2_ker
             r5 = b[5];
             r6 = b[6];
         }
-        __syncthreads();
-        // ---- step B: a_{k-1} at (x, y, p - 1) of the owned tile
+        // ---- step B: a_{k-1} at (x, y, p - 1) of the owned tile.  Its
+        // forward values do not depend on step A: loaded before the barrier,
+        // they arrive while the block waits there.
         const int q = p - 1;
-        if (owned && q >= zi0) {
-            const unsigned site = (unsigned)q * plane + col;
-            const uint8_t b8 = (own_fluid && q >= 2 && q <= dim - 3) ? (uint8_t)0 : __ldg(a.map + site);
+        const bool do_b = owned && q >= zi0;
+        const unsigned site_b = (unsigned)q * plane + col;
+        float gb[Q];
+        uint8_t b8b = 0;
+        if (do_b) {  // owned sites are never walls
+            b8b = (own_fluid && q >= 2 && q <= dim - 3) ? (uint8_t)0 : __ldg(a.map + site_b);
+            adjoint_pull<S>(fwd_b, a.off_down, site_b, gb);
+        }
+        __syncthreads();
+        if (do_b) {
+            const unsigned site = site_b;
+            const uint8_t b8 = b8b;
             // plane q + ez_i of population i: p (ez = +1), p - 1 (0), p - 2 (-1)
             const int m2 = p & 1, m3 = (p + 2) % 3, m4 = (p + 2) & 3;
             float b[Q];
@@ -499,16 +515,11 @@ __global__ void __launch_bounds__(ADJ2_EX * ADJ2_EY, LBM_ADJ2_MINB) adjoint2_ker
             b[0] = r0_prev;
             b[5] = r5_prev2;
             b[6] = r6;
-            if (b8 & M_WALL) {
-#pragma unroll
-                for (int i = 0; i < Q; ++i) b[i] = 0.f;
-            } else {
-                float d = 0.f, l = 0.f;
-                const float lidv = (b8 & M_FRONT) ? lid[col] : 0.f;
-                adjoint_site<S>(fwd_b, a.off_down, site, b8, lidv, omega, W, b, d, l);
-                dw += d;
-                dl += l;
-            }
+            float d = 0.f, l = 0.f;
+            const float lidv = (b8 & M_FRONT) ? lid[col] : 0.f;
+            adjoint_site<S>(gb, b8, lidv, omega, W, b, d, l);
+            dw += d;
+            dl += l;
 #pragma unroll
             for (int i = 0; i < Q; ++i) a.aout[site + a.off_own[i]] = b[i];
         }
