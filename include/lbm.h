@@ -94,6 +94,9 @@ typedef struct lbm_config {
     int stages;                /* TMA-staged kernel: pipeline depth (0 = tuned default)    */
     int adjoint_steps;         /* adjoint steps per launch of the backward sweep: 0 = tuned
                                   default (2 for the FP32 adjoint, 1 for FP64), 1, or 2     */
+    int adjoint_max_states;    /* > 0: at most this many recomputed state buffers in the
+                                  backward sweep (fewer than checkpoint_every - 1 makes it
+                                  checkpoint segments recursively); 0 = as many as fit     */
 } lbm_config;
 
 /* Iteration kernel variants (same results, different data movement). */

@@ -48,6 +48,7 @@ class Config(C.Structure):
         ("kernel", C.c_int),
         ("stages", C.c_int),
         ("adjoint_steps", C.c_int),
+        ("adjoint_max_states", C.c_int),
     ]
 
 
@@ -117,12 +118,13 @@ class Lattice:
     precision: "fp32" | "fp64" | "fp16" | "bf16".  stride: CSoA stride of F
     dumps (None = dim^3).  lid: optional per-column lid u_x, shape (dim, dim)
     indexed [y, x] or flat x + y*dim.  adjoint_steps: adjoint steps per
-    launch of the backward sweep (0 = default, 1, 2).
+    launch of the backward sweep (0 = default, 1, 2).  adjoint_max_states:
+    cap on the backward sweep's recomputed state buffers (0 = as many as fit).
     """
 
     def __init__(self, dim, viscosity=0.0089, velocity=0.05, precision="fp32", stride=None, lid=None,
                  seed=0, noise_sigma=0.0, tau=0.0, block_threads=0, max_device_bytes=0, device=0,
-                 profile_steps=False, kernel=0, stages=0, adjoint_steps=0):
+                 profile_steps=False, kernel=0, stages=0, adjoint_steps=0, adjoint_max_states=0):
         L = lib()
         c = default_config()
         c.dim = int(dim)
@@ -144,6 +146,7 @@ class Lattice:
         c.kernel = KERNELS[kernel] if isinstance(kernel, str) else int(kernel)
         c.stages = int(stages)
         c.adjoint_steps = int(adjoint_steps)
+        c.adjoint_max_states = int(adjoint_max_states)
         self.cfg = c
         self.dim = int(dim)
         self.n = self.dim ** 3

@@ -9,7 +9,9 @@
 // checkpoint, recomputes the segment's intermediate states with the forward
 // kernel, and applies the adjoint step from the segment's last iteration to
 // its first, two steps per launch for the FP32 adjoint (a segment of odd
-// length ends with one single step).  Memory: ceil(T/c) checkpoints + (c - 1) segment states, i.e.
+// length ends with one single step).  When the segment's states do not fit
+// in device memory, the segment itself is checkpointed and swept recursively
+// (one more forward pass per level).  Memory: ceil(T/c) checkpoints + (c - 1) segment states, i.e.
 // about 2 sqrt(T) states for c = sqrt(T); one extra forward iteration per
 // iteration of the backward sweep.
 #include <algorithm>
@@ -231,6 +233,105 @@ void free_tracked(lbm_t *h, void *p, size_t bytes)
     h->adj.bytes -= bytes;
 }
 
+// The adjoint steps k = start + len - 1 .. start with Q_k given by state(k).
+template <class State>
+int adjoint_steps_down(lbm_t *h, int start, int len, State state, int &cur)
+{
+    lbm_adjoint_state &s = h->adj;
+    int k = start + len - 1;
+    if (two_step(h)) {
+        for (; k - 1 >= start; k -= 2) {
+            ADJ_CUDA(adjoint_two_steps(h, state(k), state(k - 1), s.adj[cur], s.adj[cur ^ 1]));
+            cur ^= 1;
+        }
+    }
+    for (; k >= start; --k) {
+        lbm::AdjArgs b = adj_args(h);
+        b.fwd = state(k);
+        b.ain = s.adj[cur];
+        b.aout = s.adj[cur ^ 1];
+        ADJ_CUDA(adjoint_step(h, b));
+        cur ^= 1;
+    }
+    return LBM_OK;
+}
+
+// Backward sweep over the iterations [start, start + len), Q_start in q0,
+// with the state buffers pool[p0, p1) free.  When len - 1 buffers are free
+// the segment is recomputed and stored whole; otherwise the sweep keeps
+// sub-checkpoints every c2 iterations (c2 = ceil(sqrt(len)), wider when the
+// pool is short) and recurses into the sub-segments, last to first:
+// multi-level checkpointing, one more forward pass per level.
+int sweep(lbm_t *h, const void *q0, int start, int len, const std::vector<void *> &pool, int p0, int p1, int &cur)
+{
+    const int nfree = p1 - p0;
+    if (len - 1 <= nfree) {
+        for (int m = 1; m < len; ++m)
+            ADJ_CUDA(lbm::launch_iteration(h, m == 1 ? q0 : pool[p0 + m - 2], pool[p0 + m - 1]));
+        return adjoint_steps_down(h, start, len, [&](int k) -> const void * {
+            return k == start ? q0 : pool[p0 + (k - start) - 1];
+        }, cur);
+    }
+    if (nfree < 2)
+        return fail(LBM_ENOMEM, "adjoint: %d free state buffers are too few for a segment of %d iterations", nfree,
+                    len);
+    if (nfree < 4) {
+        // two buffers: every state recomputed from q0 (len^2 / 2 iterations)
+        void *tmp[2] = {pool[p0], pool[p0 + 1]};
+        auto advance = [&](int to, const void *&at, int &t) -> int {  // to >= t
+            for (; t < to; ++t) {
+                void *out = at == tmp[0] ? tmp[1] : tmp[0];
+                ADJ_CUDA(lbm::launch_iteration(h, at, out));
+                at = out;
+            }
+            return LBM_OK;
+        };
+        int k = start + len - 1;
+        while (k >= start) {
+            const void *at = q0;
+            int t = start;
+            const bool pair = two_step(h) && k - 1 >= start;
+            int rc = advance(pair ? k - 1 : k, at, t);
+            if (rc != LBM_OK) return rc;
+            if (pair) {
+                const void *prev = at;
+                rc = advance(k, at, t);
+                if (rc != LBM_OK) return rc;
+                rc = adjoint_steps_down(h, k - 1, 2, [&](int i) -> const void * { return i == k ? at : prev; }, cur);
+                k -= 2;
+            } else {
+                rc = adjoint_steps_down(h, k, 1, [&](int) -> const void * { return at; }, cur);
+                k -= 1;
+            }
+            if (rc != LBM_OK) return rc;
+        }
+        return LBM_OK;
+    }
+    // m sub-checkpoints after q0, two buffers left for the sub-segments
+    int c2 = (int)std::ceil(std::sqrt((double)len));
+    int m = (len + c2 - 1) / c2 - 1;
+    if (m > nfree - 2) {
+        m = nfree - 2;
+        c2 = (len + m) / (m + 1);
+        m = (len + c2 - 1) / c2 - 1;
+    }
+    // advance from q0, writing sub-checkpoint i (iteration start + i c2) into
+    // pool[p0 + i - 1] and the iterations between into two scratch buffers
+    void *tmp[2] = {pool[p0 + m], pool[p0 + m + 1]};
+    const void *at = q0;
+    for (int t = 1; t <= m * c2; ++t) {
+        void *out = (t % c2 == 0) ? pool[p0 + t / c2 - 1] : (at == tmp[0] ? tmp[1] : tmp[0]);
+        ADJ_CUDA(lbm::launch_iteration(h, at, out));
+        at = out;
+    }
+    for (int i = m; i >= 0; --i) {
+        const void *q = i == 0 ? q0 : pool[p0 + i - 1];
+        const int rc = sweep(h, q, start + i * c2, std::min(c2, len - i * c2), pool, p0 + m, p1, cur);
+        if (rc != LBM_OK) return rc;
+    }
+    return LBM_OK;
+}
+
 }  // namespace
 
 namespace lbm {
@@ -393,41 +494,32 @@ int lbm_adjoint_backward(lbm_t *h, double dloss, double *grad_tau, double *grad_
     a.dloss = m > 0 ? dloss * 2.0 / m : 0.0;
     ADJ_CUDA(loss_seed(h, a));
 
-    // segment states (c - 1), allocated on the first backward sweep only, so
-    // a loss-only forward holds just its checkpoints
+    // segment states: c - 1 when they fit (one-level sqrt checkpointing),
+    // else as many as fit, and the sweep recurses.  Allocated on the first
+    // backward sweep only, so a loss-only forward holds just its checkpoints.
     const int T = s.iterations, c = s.every;
     const size_t fbytes = (size_t)lbm::Q * h->n * lbm::storage_bytes(h->prec);
-    while ((int)s.seg.size() < c - 1) {
-        void *p = nullptr;
-        int rc = alloc_tracked(h, &p, fbytes);
-        if (rc != LBM_OK) return rc;
-        s.seg.push_back(p);
+    if ((int)s.seg.size() < c - 1) {
+        size_t freeb = 0, totalb = 0;
+        ADJ_CUDA(cudaMemGetInfo(&freeb, &totalb));
+        const size_t margin = ((size_t)1 << 30) + totalb / 50;  // for the runtime and other users
+        const size_t fit = freeb > margin ? (freeb - margin) / fbytes : 0;
+        size_t want_total = (size_t)(c - 1);
+        if (h->cfg.adjoint_max_states > 0) want_total = std::min(want_total, (size_t)h->cfg.adjoint_max_states);
+        const int want =
+            want_total > s.seg.size() ? (int)std::min<size_t>(want_total - s.seg.size(), fit) : 0;
+        for (int k = 0; k < want; ++k) {
+            void *p = nullptr;
+            if (alloc_tracked(h, &p, fbytes) != LBM_OK) break;  // budget reached: recurse with fewer
+            s.seg.push_back(p);
+        }
     }
     // segments, last to first
     const int nck = (T + c - 1) / c;
     for (int j = nck - 1; j >= 0; --j) {
-        const int start = j * c, end = std::min(T, start + c);
-        for (int k = start + 1; k < end; ++k) {
-            const void *fin = (k - 1 == start) ? s.ckpt[j] : s.seg[k - 2 - start];
-            ADJ_CUDA(lbm::launch_iteration(h, fin, s.seg[k - 1 - start]));
-        }
-        // Q_k of this segment
-        auto state = [&](int k) -> const void * { return k == start ? s.ckpt[j] : s.seg[k - 1 - start]; };
-        int k = end - 1;
-        if (two_step(h)) {
-            for (; k - 1 >= start; k -= 2) {
-                ADJ_CUDA(adjoint_two_steps(h, state(k), state(k - 1), s.adj[cur], s.adj[cur ^ 1]));
-                cur ^= 1;
-            }
-        }
-        for (; k >= start; --k) {
-            lbm::AdjArgs b = adj_args(h);
-            b.fwd = state(k);
-            b.ain = s.adj[cur];
-            b.aout = s.adj[cur ^ 1];
-            ADJ_CUDA(adjoint_step(h, b));
-            cur ^= 1;
-        }
+        const int start = j * c, len = std::min(T, start + c) - start;
+        const int rc = sweep(h, s.ckpt[j], start, len, s.seg, 0, (int)s.seg.size(), cur);
+        if (rc != LBM_OK) return rc;
     }
     // a_0 = dJ/dR_0; the init kernel's lid dependence of R_0
     if (s.init_state) {

@@ -320,6 +320,8 @@ int lbm_init(lbm_t **out, const lbm_config *c)
     if (c->stages < 0 || c->stages > 16) return fail(LBM_EINVAL, "lbm_init: stages %d out of range", c->stages);
     if (c->adjoint_steps < 0 || c->adjoint_steps > 2)
         return fail(LBM_EINVAL, "lbm_init: adjoint_steps %d out of range (0, 1, 2)", c->adjoint_steps);
+    if (c->adjoint_max_states < 0)
+        return fail(LBM_EINVAL, "lbm_init: adjoint_max_states %d must be >= 0", c->adjoint_max_states);
     if (c->block_threads < 0 || c->block_threads > 1024)
         return fail(LBM_EINVAL, "lbm_init: block_threads %d out of range", c->block_threads);
     if (c->lid_profile) {

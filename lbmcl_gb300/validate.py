@@ -216,11 +216,22 @@ def lidfield(args):
                 "adjoint_over_forward": round((t2 - t1) * 1e3 / steps / fwd_ms, 3),
                 "device_gb_used_peak": round((free0 - min(free1, free2)) / 1e9, 2)})
     if args.fp64_adjoint:
+        # FP64 states are 4x the 16-bit ones: wider top-level checkpoints, and
+        # the backward sweep checkpoints each segment again as memory requires
+        c64 = args.fp64_every
+        free_a, _ = torch.cuda.mem_get_info()
         with capi.Lattice(dim, velocity=0.0, precision="fp64", lid=lid, tau=tau, stride=0) as L:
             L.adjoint_set_loss(plane, target)
-            J64 = L.adjoint_forward(steps, c)
+            t0 = time.perf_counter()
+            J64 = L.adjoint_forward(steps, c64)
+            t1 = time.perf_counter()
             gt64, gl64, _ = L.adjoint_backward(1.0, want_f0=False)
+            t2 = time.perf_counter()
+            free_b, _ = torch.cuda.mem_get_info()
         act = (slice(2, dim - 2), slice(2, dim - 2))
+        out["fp64_adjoint_run"] = {"checkpoint_every": c64, "forward_s": round(t1 - t0, 1),
+                                   "backward_s": round(t2 - t1, 1),
+                                   "device_gb_used": round((free_a - free_b) / 1e9, 1)}
         out["vs_fp64_adjoint"] = {"loss_fp64": J64,
                                   "lid_rel_l2": float(np.linalg.norm(gl[act] - gl64[act]) / np.linalg.norm(gl64[act])),
                                   "tau_rel": abs(gt - gt64) / abs(gt64)}
@@ -261,6 +272,7 @@ def main(argv=None) -> int:
     p.add_argument("--columns", type=int, default=8)
     p.add_argument("--precision", default="fp16")
     p.add_argument("--fp64-adjoint", action="store_true")
+    p.add_argument("--fp64-every", type=int, default=500, help="top-level checkpoint interval of the FP64 adjoint")
     p.add_argument("--seed", type=int, default=1234)
     a = ap.parse_args(argv)
     {"storage": storage, "adjoint": adjoint, "lidfield": lidfield}[a.cmd](a)

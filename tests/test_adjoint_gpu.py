@@ -109,6 +109,44 @@ def test_fp32_adjoint_close_to_fp64(capi, prec):
     assert np.linalg.norm(g[1] - g64[1]) <= tol * np.linalg.norm(g64[1])
 
 
+@pytest.mark.parametrize("states,steps", [(2, 1), (3, 1), (5, 1), (9, 1), (3, 2), (6, 2)])
+def test_recursive_checkpointing(capi, states, steps):
+    """With fewer state buffers than a segment needs, the backward sweep
+    checkpoints the segment recursively (2-3 buffers: every state recomputed
+    from the checkpoint).  One step per launch: the same launches on the same
+    states as the stored trajectory, so the gradients are bit for bit equal;
+    two steps per launch pair the steps differently (sums in another order)."""
+    dim, iters, every = 16, 45, 45
+    lid, target = setup_case(dim, 11)
+    res = {}
+    for cap in (0, states):
+        with capi.Lattice(dim, velocity=0.0, precision="fp32", lid=lid, tau=0.53, seed=5, noise_sigma=1e-4,
+                          adjoint_steps=steps, adjoint_max_states=cap) as L:
+            L.adjoint_set_loss(8, target)
+            J = L.adjoint_forward(iters, every if cap else 1)
+            res[cap] = (J,) + tuple(L.adjoint_backward(1.0))
+    (J0, t0, l0, f0), (J1, t1, l1, f1) = res[0], res[states]
+    assert J0 == J1
+    if steps == 1:
+        assert t0 == t1
+        np.testing.assert_array_equal(l0, l1)
+        np.testing.assert_array_equal(f0, f1)
+    else:
+        assert abs(t1 - t0) <= 1e-5 * abs(t0)
+        assert np.abs(l1 - l0).max() <= 1e-5 * np.abs(l0).max()
+        assert np.abs(f1 - f0).max() <= 1e-5 * np.abs(f0).max()
+
+
+def test_recursive_checkpointing_refuses_one_buffer(capi):
+    dim = 16
+    lid, target = setup_case(dim, 12)
+    with capi.Lattice(dim, velocity=0.0, precision="fp32", lid=lid, tau=0.53, adjoint_max_states=1) as L:
+        L.adjoint_set_loss(8, target)
+        L.adjoint_forward(10, 10)
+        with pytest.raises(capi.LbmError, match="too few"):
+            L.adjoint_backward(1.0)
+
+
 @pytest.mark.parametrize("prec", ["fp32", "fp16", "bf16"])
 @pytest.mark.parametrize("dim,iters,every", [(16, 23, 6), (40, 17, 17), (64, 12, 4)])
 def test_two_step_adjoint_matches_one_step(capi, prec, dim, iters, every):

@@ -50,6 +50,7 @@ def _init(libonly, **kw):
     (dict(block_threads=4096), "block_threads"),
     (dict(adjoint_steps=3), "adjoint_steps"),
     (dict(adjoint_steps=-1), "adjoint_steps"),
+    (dict(adjoint_max_states=-2), "adjoint_max_states"),
 ])
 def test_init_rejects_bad_arguments(libonly, kw, frag):
     rc, msg = _init(libonly, **kw)
