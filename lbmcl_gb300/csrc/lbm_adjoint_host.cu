@@ -506,6 +506,13 @@ int lbm_adjoint_backward(lbm_t *h, double dloss, double *grad_tau, double *grad_
         const size_t fit = freeb > margin ? (freeb - margin) / fbytes : 0;
         size_t want_total = (size_t)(c - 1);
         if (h->cfg.adjoint_max_states > 0) want_total = std::min(want_total, (size_t)h->cfg.adjoint_max_states);
+        if (want_total > s.seg.size() + fit) {
+            // a whole segment does not fit: take what the two-level schedule
+            // uses (sub-checkpoints + one sub-segment + two), not all memory
+            const size_t c2 = (size_t)std::ceil(std::sqrt((double)c));
+            const size_t two_level = ((size_t)c + c2 - 1) / c2 - 1 + (c2 - 1) + 2;
+            want_total = std::min(want_total, std::max<size_t>(two_level, 4));
+        }
         const int want =
             want_total > s.seg.size() ? (int)std::min<size_t>(want_total - s.seg.size(), fit) : 0;
         for (int k = 0; k < want; ++k) {
