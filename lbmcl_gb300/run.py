@@ -25,12 +25,14 @@ def main(argv=None) -> int:
     ap.add_argument("--kernel", default="auto", choices=sorted(capi.KERNELS))
     ap.add_argument("--stages", type=int, default=0)
     ap.add_argument("--adjoint-steps", type=int, default=0, help="adjoint steps per launch (0 = default)")
+    ap.add_argument("--adjoint-max-states", type=int, default=0, help="cap on the backward sweep's state buffers")
     ap.add_argument("--adjoint", default="", help="T,c: also run an adjoint forward/backward of T iterations, "
                                                   "checkpoint every c")
     a = ap.parse_args(argv)
     with capi.Lattice(a.dim, a.viscosity, a.velocity, precision=a.precision, stride=0, seed=a.seed,
                       noise_sigma=a.noise, block_threads=a.block, profile_steps=True, kernel=a.kernel,
-                      stages=a.stages, adjoint_steps=a.adjoint_steps) as L:
+                      stages=a.stages, adjoint_steps=a.adjoint_steps,
+                      adjoint_max_states=a.adjoint_max_states) as L:
         t0 = time.perf_counter()
         L.step(a.steps, every=a.every)
         L.sync()
