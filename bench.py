@@ -61,6 +61,24 @@ def dist_env():
     return ws, rank, local
 
 
+def slowest_rank_ms(ms: float, ws: int, device: str = "cpu") -> float:
+    """The step time of the slowest rank (max over ranks); each rank runs its
+    own replica, so the job's time is the slowest one's."""
+    if ws <= 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_mlups(wet_sites: int, ms_slowest: float, ws: int) -> float:
+    """Whole-job throughput of ws replicas: every rank updates wet_sites per
+    step, in the slowest rank's time (weak scaling)."""
+    return wet_sites * ws / (ms_slowest * 1e3)
+
+
 class ClockSampler:
     """nvidia-smi SM clock / throttle-reason samples while running."""
 
@@ -347,14 +365,11 @@ def main():
         k = args.steps if m == modes[0] else (max(10, args.steps // 5) if m != "fp64" else max(5, args.steps // 50))
         ms = time_mode(capi, m, k, args.warmup if m != "fp64" else 3, device, barrier,
                        sampler if m == modes[0] else None)
-        if ws > 1:
-            import torch.distributed as dist
-            t = torch.tensor([ms], device=f"cuda:{device}")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = slowest_rank_ms(ms, ws, f"cuda:{device}")
         mlups = wet / (ms * 1e3)
         gbs = wet * BYTES_PER_SITE[m] / (ms * 1e-3) / 1e9
-        res[m] = {"mlups": round(mlups * ws, 1), "mlups_per_gpu": round(mlups, 1), "ms_per_step": round(ms, 4),
+        res[m] = {"mlups": round(job_mlups(wet, ms, ws), 1), "mlups_per_gpu": round(mlups, 1),
+                  "ms_per_step": round(ms, 4),
                   "gbs": round(gbs, 1), "frac_hbm": round(gbs / peak, 4), "steps": k}
 
     head = modes[0]
