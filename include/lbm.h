@@ -16,6 +16,9 @@
  *   - A handle owns all device memory and one CUDA stream.  lbm_step is
  *     asynchronous on that stream; lbm_dump, lbm_load, lbm_sync, lbm_timing
  *     and lbm_reduce synchronise it.  Use one handle per host thread.
+ *   - Every call on a handle runs on the handle's device (lbm_config.device)
+ *     and leaves the caller's current device as it found it; lbm_init makes
+ *     the handle's device current.
  *   - Host buffers passed in are caller-owned; the library never keeps them.
  *   - Iteration labels follow the reference host (lbmcl.hpp:435-520): after
  *     lbm_step has run t iterations in total, an F dump holds the buffer that

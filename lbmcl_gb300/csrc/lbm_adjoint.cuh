@@ -386,7 +386,6 @@ struct Adj2Args {
     const void *lid;     // forward macro type, dim*dim
     double *grad_lid;    // dim*dim
     double *tau_acc;     // per block
-    unsigned n;          // dim^3
     int dim;
     int ntx, nty;        // tiles in x and y
     int zc;              // planes per chunk

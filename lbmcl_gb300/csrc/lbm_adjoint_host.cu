@@ -131,13 +131,11 @@ unsigned adj2_grid(const lbm_t *h, int &ntx, int &nty)
 template <class S>
 cudaError_t run_adjoint2(const lbm::Adj2Args &a, unsigned grid, cudaStream_t s)
 {
-    static bool attr = false;  // per process: the attribute is per function, not per device
-    if (!attr) {
-        const cudaError_t e = cudaFuncSetAttribute(lbm::adjoint2_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                   (int)lbm::ADJ2_SMEM);
-        if (e != cudaSuccess) return e;
-        attr = true;
-    }
+    // set on every launch: the attribute belongs to the current device's
+    // context, and handles may live on different devices and threads
+    const cudaError_t e = cudaFuncSetAttribute(lbm::adjoint2_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)lbm::ADJ2_SMEM);
+    if (e != cudaSuccess) return e;
     lbm::adjoint2_kernel<S><<<grid, lbm::ADJ2_EX * lbm::ADJ2_EY, lbm::ADJ2_SMEM, s>>>(a);
     return cudaGetLastError();
 }
@@ -154,7 +152,6 @@ cudaError_t adjoint_two_steps(const lbm_t *h, const void *fwd_a, const void *fwd
     a.lid = h->lid;
     a.grad_lid = h->adj.grad_lid;
     a.tau_acc = h->adj.tau_acc;
-    a.n = (unsigned)h->n;
     a.dim = h->dim;
     a.zc = kAdj2Chunk;
     for (int i = 0; i < lbm::Q; ++i) {
@@ -362,6 +359,7 @@ extern "C" {
 int lbm_adjoint_set_loss(lbm_t *h, int plane_y, const double *target_ux)
 {
     if (!h) return fail(LBM_EINVAL, "lbm_adjoint_set_loss: NULL handle");
+    const lbm::DeviceScope dev(h->cfg.device);
     if (plane_y < 2 || plane_y > h->dim - 3)
         return fail(LBM_EINVAL, "lbm_adjoint_set_loss: plane_y %d must hold FLUID sites ([2, %d])", plane_y,
                     h->dim - 3);
@@ -386,6 +384,7 @@ int lbm_adjoint_set_loss(lbm_t *h, int plane_y, const double *target_ux)
 int lbm_adjoint_forward(lbm_t *h, int iterations, int checkpoint_every, double *loss)
 {
     if (!h) return fail(LBM_EINVAL, "lbm_adjoint_forward: NULL handle");
+    const lbm::DeviceScope dev(h->cfg.device);
     if (iterations < 1 || checkpoint_every < 1)
         return fail(LBM_EINVAL, "lbm_adjoint_forward: iterations and checkpoint_every must be >= 1");
     if (h->adj.plane_y < 0) return fail(LBM_ESTATE, "lbm_adjoint_forward: call lbm_adjoint_set_loss first");
@@ -450,6 +449,7 @@ int lbm_adjoint_backward(lbm_t *h, double dloss, double *grad_tau, double *grad_
                          size_t grad_f0_bytes)
 {
     if (!h) return fail(LBM_EINVAL, "lbm_adjoint_backward: NULL handle");
+    const lbm::DeviceScope dev(h->cfg.device);
     lbm_adjoint_state &s = h->adj;
     if (!s.ready || s.it_end != h->it)
         return fail(LBM_ESTATE, "lbm_adjoint_backward: no adjoint forward recorded for the current state");

@@ -129,6 +129,7 @@ int fold_events(lbm_t *h, bool wait)
 void release(lbm_t *h)
 {
     if (!h) return;
+    const lbm::DeviceScope dev(h->cfg.device);
     if (h->stream) cudaStreamSynchronize(h->stream);
     lbm::release_adjoint(h);
     for (void *p : {h->f[0], h->f[1], (void *)h->map, h->rho, h->u, h->lid, h->stage, (void *)h->partials,
@@ -452,6 +453,7 @@ int lbm_init(lbm_t **out, const lbm_config *c)
 int lbm_step(lbm_t *h, int nsteps, int macro_every)
 {
     if (!h) return fail(LBM_EINVAL, "lbm_step: NULL handle");
+    const lbm::DeviceScope dev(h->cfg.device);
     if (nsteps < 0 || macro_every < 0) return fail(LBM_EINVAL, "lbm_step: nsteps and macro_every must be >= 0");
     if (nsteps == 0) return LBM_OK;
     h->state_is_init = false;
@@ -494,6 +496,7 @@ int lbm_step(lbm_t *h, int nsteps, int macro_every)
 int lbm_sync(lbm_t *h)
 {
     if (!h) return fail(LBM_EINVAL, "lbm_sync: NULL handle");
+    const lbm::DeviceScope dev(h->cfg.device);
     LBM_CUDA(cudaStreamSynchronize(h->stream));
     int st = 0;
     LBM_CUDA(cudaMemcpy(&st, h->status, sizeof(int), cudaMemcpyDeviceToHost));
@@ -504,6 +507,7 @@ int lbm_sync(lbm_t *h)
 int lbm_dump(lbm_t *h, int what, void *dst, size_t bytes)
 {
     if (!h || !dst) return fail(LBM_EINVAL, "lbm_dump: NULL argument");
+    const lbm::DeviceScope dev(h->cfg.device);
     const size_t want = lbm_size(h, what);
     if (want == 0) return fail(LBM_EINVAL, "lbm_dump: unknown quantity %d", what);
     if (bytes != want) return fail(LBM_EINVAL, "lbm_dump: buffer is %zu bytes, quantity %d needs %zu", bytes, what, want);
@@ -562,6 +566,7 @@ int lbm_dump(lbm_t *h, int what, void *dst, size_t bytes)
 int lbm_load(lbm_t *h, int what, const void *src, size_t bytes)
 {
     if (!h || !src) return fail(LBM_EINVAL, "lbm_load: NULL argument");
+    const lbm::DeviceScope dev(h->cfg.device);
     if (what != LBM_DUMP_F && what != LBM_DUMP_F_RAW)
         return fail(LBM_EINVAL, "lbm_load: only LBM_DUMP_F and LBM_DUMP_F_RAW can be loaded");
     const size_t want = lbm_size(h, what);
@@ -603,6 +608,7 @@ int lbm_load(lbm_t *h, int what, const void *src, size_t bytes)
 int lbm_timing(lbm_t *h, double *total_ms, double *kernels_ms)
 {
     if (!h) return fail(LBM_EINVAL, "lbm_timing: NULL handle");
+    const lbm::DeviceScope dev(h->cfg.device);
     LBM_CUDA(cudaStreamSynchronize(h->stream));
     int rc = fold_events(h, true);
     if (rc != LBM_OK) return rc;
@@ -627,6 +633,7 @@ const char *lbm_device_name(const lbm_t *h) { return h ? h->device_name.c_str() 
 int lbm_reduce(lbm_t *h, double out[3])
 {
     if (!h || !out) return fail(LBM_EINVAL, "lbm_reduce: NULL argument");
+    const lbm::DeviceScope dev(h->cfg.device);
     const lbm::StepArgs a = step_args(h, h->cur);
     unsigned nparts = 0;
     LBM_CUDA(launch_pull(h, lbm::MODE_REDUCE, a, &nparts));

@@ -72,6 +72,22 @@ struct lbm_handle {
 
 
 namespace lbm {
+// Makes the handle's device current for one entry point and restores the
+// caller's device afterwards (handles of several devices may share a thread).
+struct DeviceScope {
+    int prev = -1;
+    explicit DeviceScope(int dev)
+    {
+        int cur = -1;
+        if (cudaGetDevice(&cur) == cudaSuccess && cur != dev && cudaSetDevice(dev) == cudaSuccess) prev = cur;
+    }
+    ~DeviceScope()
+    {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+    DeviceScope(const DeviceScope &) = delete;
+    DeviceScope &operator=(const DeviceScope &) = delete;
+};
 // storage / macro / dump element sizes of a precision
 inline size_t storage_bytes(int prec) { return prec == LBM_FP64 ? 8 : (prec == LBM_FP32 ? 4 : 2); }
 inline size_t macro_bytes(int prec) { return prec == LBM_FP64 ? 8 : 4; }
