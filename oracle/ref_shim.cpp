@@ -9,7 +9,7 @@
  * oracle/_ref/ and is never committed.
  *
  * The OpenCL C keywords are mapped to nothing, get_global_id() reads a
- * per-thread index set by the driver loops below, and the compile-time
+ * per-thread index set by the loops over sites below, and the compile-time
  * macros the reference host passes with -D (lbmcl.hpp:131-156) become
  * run-time globals.  VELOCITY may additionally read a per-column lid array,
  * which is valid wherever the reference uses it because x and y are in scope

@@ -1,6 +1,6 @@
 """Parity of the sm_103a library (through the C ABI) with the CPU oracle.
 
-Bars (the benchmark spec): max |df| <= 1e-5 in FP32 and <= 1e-12 in FP64 against the
+Bars: max |df| <= 1e-5 in FP32 and <= 1e-12 in FP64 against the
 oracle on identical inputs, lattice map bit-exact.  The FP32 / FP64 kernels
 evaluate every expression in the reference's operand order without FMA
 contraction, so they are also checked for bit-for-bit equality.
