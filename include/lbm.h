@@ -96,7 +96,9 @@ typedef struct lbm_config {
                                   (NARROW for FP32, DIRECT otherwise)                       */
     int stages;                /* TMA-staged kernel: pipeline depth (0 = tuned default)    */
     int adjoint_steps;         /* adjoint steps per launch of the backward sweep: 0 = tuned
-                                  default (2 for the FP32 adjoint, 1 for FP64), 1, or 2     */
+                                  default (2 for the FP32 adjoint on lattices that fill the
+                                  GPU, about 128^3 and up; else 1), 1, or 2 (FP32 adjoint,
+                                  dim <= 609)                                               */
     int adjoint_max_states;    /* > 0: at most this many recomputed state buffers in the
                                   backward sweep (fewer than checkpoint_every - 1 makes it
                                   checkpoint segments recursively); 0 = as many as fit     */

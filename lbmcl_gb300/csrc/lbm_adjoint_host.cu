@@ -114,11 +114,6 @@ cudaError_t run_lid_init_grad(const lbm::AdjArgs &a, cudaStream_t s)
 // ---- two steps per launch (FP32 adjoint)
 constexpr int kAdj2Chunk = 32;  // z-planes per block
 
-bool two_step(const lbm_t *h)
-{
-    return h->prec != LBM_FP64 && h->cfg.adjoint_steps != 1 && h->dim <= lbm::ADJ2_MAX_DIM;
-}
-
 unsigned adj2_grid(const lbm_t *h, int &ntx, int &nty)
 {
     const int m = h->dim - 2;
@@ -126,6 +121,17 @@ unsigned adj2_grid(const lbm_t *h, int &ntx, int &nty)
     nty = (m + lbm::ADJ2_TY - 1) / lbm::ADJ2_TY;
     const int ntz = (m + kAdj2Chunk - 1) / kAdj2Chunk;
     return (unsigned)ntx * (unsigned)nty * (unsigned)ntz;
+}
+
+// Two steps per launch for the FP32 adjoint (adjoint_steps 0 or 2), up to
+// ADJ2_MAX_DIM.  By default only where its grid gives every SM two blocks or
+// more: a small lattice (64^3: 66 blocks) runs faster one step at a time.
+bool two_step(const lbm_t *h)
+{
+    if (h->prec == LBM_FP64 || h->cfg.adjoint_steps == 1 || h->dim > lbm::ADJ2_MAX_DIM) return false;
+    if (h->cfg.adjoint_steps == 2) return true;
+    int ntx, nty;
+    return adj2_grid(h, ntx, nty) >= 2u * (unsigned)std::max(h->num_sms, 1);
 }
 
 template <class S>

@@ -378,6 +378,7 @@ int lbm_init(lbm_t **out, const lbm_config *c)
         cudaDeviceProp prop;
         LBM_CUDA(cudaGetDeviceProperties(&prop, c->device));
         h->device_name = prop.name;
+        h->num_sms = prop.multiProcessorCount;
         LBM_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
         LBM_CUDA(cudaEventCreate(&h->ev_first));
         LBM_CUDA(cudaEventCreate(&h->ev_last));

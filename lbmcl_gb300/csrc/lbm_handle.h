@@ -64,6 +64,7 @@ struct lbm_handle {
     unsigned ngroups = 0, sgrid = 0, sblock = 0;
     size_t ssmem = 0;
     std::string device_name;
+    int num_sms = 0;
     bool state_is_init = true;  // the populations are what lbm_init made
     size_t base_bytes = 0;      // device bytes lbm_init allocated
     lbm_adjoint_state adj;
