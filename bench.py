@@ -262,9 +262,19 @@ def host_mem_available() -> float:
     return 0.0
 
 
-def cpu_oracle_mlups(budget_s, dim=512, threads=0):
+def trimmed_mean(values):
+    """benchmark.sh:111-176: the mean without the smallest and the largest
+    value (at least three values)."""
+    v = sorted(values)
+    if len(v) < 3:
+        raise ValueError("the trimmed mean needs at least 3 values")
+    return sum(v[1:-1]) / (len(v) - 2)
+
+
+def cpu_oracle_mlups(budget_s, dim=512, threads=0, runs=10):
     """Oracle push step (FP32, all host threads) over z-slabs of a dim^3
-    lattice; returns (MLUPS, threads, description)."""
+    lattice, `runs` timed slabs and their trimmed mean (as benchmark.sh
+    aggregates its runs); returns (MLUPS, threads, description, seconds)."""
     from oracle import pyoracle as po
     po.build()
     L = po.OracleLattice(dim, WORKLOAD["viscosity"], WORKLOAD["velocity"], "f32", stride=None, threads=threads)
@@ -273,18 +283,17 @@ def cpu_oracle_mlups(budget_s, dim=512, threads=0):
     t = time.perf_counter()
     L.compute_slab(1, 9)
     per_plane = (time.perf_counter() - t) / 8
-    planes = int(max(8, min(dim - 2, budget_s / max(per_plane, 1e-9))))
-    done, secs = 0, 0.0
-    while done < planes:
-        nz = min(planes - done, dim - 2)
+    planes = int(max(8, min(dim - 2, budget_s / runs / max(per_plane, 1e-9))))
+    times = []
+    for _ in range(runs):
         t = time.perf_counter()
-        L.compute_slab(1, 1 + nz)
-        secs += time.perf_counter() - t
-        done += nz
-    sites = done * dim * dim
-    desc = (f"oracle C restatement of kernels.cl, FP32, OpenMP {nthreads} threads, {done} z-planes "
-            f"({sites / 1e6:.1f} M site updates) of a {dim}^3 lattice")
-    return sites / secs / 1e6, nthreads, desc, secs
+        L.compute_slab(1, 1 + planes)
+        times.append(time.perf_counter() - t)
+    secs = trimmed_mean(times)
+    sites = planes * dim * dim
+    desc = (f"oracle C restatement of kernels.cl, FP32, OpenMP {nthreads} threads, {planes} z-planes "
+            f"({sites / 1e6:.1f} M site updates) of a {dim}^3 lattice per run, trimmed mean of {runs} runs")
+    return sites / secs / 1e6, nthreads, desc, sum(times)
 
 
 def run_reference(args):

@@ -62,3 +62,12 @@ def test_reference_arm_other_ranks_exit_without_work(monkeypatch):
     monkeypatch.setenv("RANK", "1")
     monkeypatch.setenv("LOCAL_RANK", "1")
     assert bench.run_reference(argparse.Namespace(steps=3, warmup=3, gpus=2)) == 0
+
+
+def test_trimmed_mean_is_benchmark_sh():
+    sys.path.insert(0, ROOT)
+    import bench
+    assert bench.trimmed_mean([5.0, 1.0, 3.0, 9.0, 4.0]) == 4.0   # drops 1 and 9
+    assert bench.trimmed_mean([2.0, 2.0, 2.0]) == 2.0
+    with pytest.raises(ValueError):
+        bench.trimmed_mean([1.0, 2.0])
