@@ -162,7 +162,10 @@ def adjoint(args):
     print(json.dumps(out), flush=True)
 
 
-def _smooth_lid(dim, rng, amplitude=0.02, base=0.05):
+def smooth_lid(dim, rng, amplitude=0.02, base=0.05):
+    """A smooth lid field [y, x]: base + the sum of four seeded 2-D sinusoids
+    (wave numbers 1..3, random phases) scaled to a peak deviation of
+    `amplitude`."""
     x = np.arange(dim) / dim
     X, Y = np.meshgrid(x, x)  # [y, x]
     f = np.zeros((dim, dim))
@@ -181,7 +184,7 @@ def lidfield(args):
     tau = 3 * nu + 0.5
     plane = dim // 2
     rng = np.random.default_rng(args.seed)
-    target_lid = _smooth_lid(dim, rng).reshape(-1)
+    target_lid = smooth_lid(dim, rng).reshape(-1)
     with capi.Lattice(dim, nu, 0.05, precision="fp32", lid=target_lid, stride=0) as L:
         L.step(steps)
         L.step(1, every=steps + 1)
