@@ -102,6 +102,10 @@ typedef struct lbm_config {
     int adjoint_max_states;    /* > 0: at most this many recomputed state buffers in the
                                   backward sweep (fewer than checkpoint_every - 1 makes it
                                   checkpoint segments recursively); 0 = as many as fit     */
+    int graph_iterations;      /* lbm_step replays runs of this many plain iterations as
+                                  one captured CUDA graph (launch-bound small lattices);
+                                  0 = default 16, 1 = launch every kernel directly; an
+                                  even number, at most 256                                  */
 } lbm_config;
 
 /* Iteration kernel variants (same results, different data movement). */

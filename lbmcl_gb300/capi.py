@@ -49,6 +49,7 @@ class Config(C.Structure):
         ("stages", C.c_int),
         ("adjoint_steps", C.c_int),
         ("adjoint_max_states", C.c_int),
+        ("graph_iterations", C.c_int),
     ]
 
 
@@ -120,11 +121,14 @@ class Lattice:
     indexed [y, x] or flat x + y*dim.  adjoint_steps: adjoint steps per
     launch of the backward sweep (0 = default, 1, 2).  adjoint_max_states:
     cap on the backward sweep's recomputed state buffers (0 = as many as fit).
+    graph_iterations: iterations per CUDA graph replay in step() (0 = 16,
+    1 = no graphs).
     """
 
     def __init__(self, dim, viscosity=0.0089, velocity=0.05, precision="fp32", stride=None, lid=None,
                  seed=0, noise_sigma=0.0, tau=0.0, block_threads=0, max_device_bytes=0, device=0,
-                 profile_steps=False, kernel=0, stages=0, adjoint_steps=0, adjoint_max_states=0):
+                 profile_steps=False, kernel=0, stages=0, adjoint_steps=0, adjoint_max_states=0,
+                 graph_iterations=0):
         L = lib()
         c = default_config()
         c.dim = int(dim)
@@ -147,6 +151,7 @@ class Lattice:
         c.stages = int(stages)
         c.adjoint_steps = int(adjoint_steps)
         c.adjoint_max_states = int(adjoint_max_states)
+        c.graph_iterations = int(graph_iterations)
         self.cfg = c
         self.dim = int(dim)
         self.n = self.dim ** 3

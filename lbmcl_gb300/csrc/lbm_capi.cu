@@ -140,6 +140,8 @@ void release(lbm_t *h)
         cudaEventDestroy(p.second);
     }
     for (auto e : h->spare) cudaEventDestroy(e);
+    for (cudaGraphExec_t &g : h->graph_exec)
+        if (g) cudaGraphExecDestroy(g), g = nullptr;
     if (h->ev_first) cudaEventDestroy(h->ev_first);
     if (h->ev_last) cudaEventDestroy(h->ev_last);
     if (h->stream) cudaStreamDestroy(h->stream);
@@ -246,6 +248,42 @@ cudaError_t launch_pull(const lbm_t *h, int mode, const lbm::StepArgs &a, unsign
 
 size_t dump_elem(int prec) { return prec == LBM_FP64 ? 8 : 4; }
 
+// true when one of the iterations it0 + 1 .. it0 + G stores the moments
+bool macro_within(int64_t it0, int G, int macro_every)
+{
+    if (macro_every == 0) return false;
+    const int64_t next = (it0 / macro_every + 1) * macro_every;  // first macro iteration after it0
+    return next <= it0 + G;
+}
+
+// Replay (capturing on first use) the graph of h->graph_iters plain
+// iterations that starts from buffer h->cur.  The kernels' arguments are
+// fixed per parity (the two buffers ping-pong), so two graphs cover every
+// call.
+cudaError_t replay_graph(lbm_t *h)
+{
+    cudaGraphExec_t &exec = h->graph_exec[h->cur];
+    if (!exec) {
+        cudaError_t e = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) return e;
+        int cur = h->cur;
+        for (int k = 0; k < h->graph_iters && e == cudaSuccess; ++k) {
+            e = launch_pull(h, lbm::MODE_STEP, step_args(h, cur));
+            cur ^= 1;
+        }
+        cudaGraph_t g = nullptr;
+        const cudaError_t ec = cudaStreamEndCapture(h->stream, &g);
+        if (e == cudaSuccess) e = ec;
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, g, 0);
+        if (g) cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            exec = nullptr;
+            return e;
+        }
+    }
+    return cudaGraphLaunch(exec, h->stream);
+}
+
 }  // namespace
 
 namespace lbm {
@@ -323,6 +361,9 @@ int lbm_init(lbm_t **out, const lbm_config *c)
         return fail(LBM_EINVAL, "lbm_init: adjoint_steps %d out of range (0, 1, 2)", c->adjoint_steps);
     if (c->adjoint_max_states < 0)
         return fail(LBM_EINVAL, "lbm_init: adjoint_max_states %d must be >= 0", c->adjoint_max_states);
+    if (c->graph_iterations < 0 || c->graph_iterations > 256 || (c->graph_iterations > 1 && c->graph_iterations % 2))
+        return fail(LBM_EINVAL, "lbm_init: graph_iterations %d must be 0, 1 or an even number <= 256",
+                    c->graph_iterations);
     if (c->block_threads < 0 || c->block_threads > 1024)
         return fail(LBM_EINVAL, "lbm_init: block_threads %d out of range", c->block_threads);
     if (c->lid_profile) {
@@ -379,6 +420,7 @@ int lbm_init(lbm_t **out, const lbm_config *c)
         LBM_CUDA(cudaGetDeviceProperties(&prop, c->device));
         h->device_name = prop.name;
         h->num_sms = prop.multiProcessorCount;
+        h->graph_iters = c->graph_iterations == 0 ? 16 : c->graph_iterations;
         LBM_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
         LBM_CUDA(cudaEventCreate(&h->ev_first));
         LBM_CUDA(cudaEventCreate(&h->ev_last));
@@ -468,7 +510,17 @@ int lbm_step(lbm_t *h, int nsteps, int macro_every)
         LBM_CUDA(get_event(h, &e1));
         LBM_CUDA(cudaEventRecord(e0, h->stream));
     }
-    for (int k = 0; k < nsteps; ++k) {
+    for (int k = 0; k < nsteps;) {
+        // a run of graph_iters plain iterations (no macro output, no
+        // per-iteration events) replays the captured graph of this parity
+        const int G = h->graph_iters;
+        if (!per_step && G > 1 && nsteps - k >= G && !macro_within(h->it, G, macro_every)) {
+            LBM_CUDA(replay_graph(h));
+            k += G;
+            h->it += G;  // G is even: h->cur is unchanged
+            continue;
+        }
+        ++k;
         const int64_t it = h->it + 1;
         const bool macro = macro_every != 0 && (it % macro_every) == 0;
         const lbm::StepArgs a = step_args(h, h->cur);

@@ -65,6 +65,10 @@ struct lbm_handle {
     size_t ssmem = 0;
     std::string device_name;
     int num_sms = 0;
+    // lbm_step: graph_iters plain iterations captured once per starting
+    // buffer parity and replayed (graph_iters = 1: no graphs)
+    int graph_iters = 16;
+    cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};
     bool state_is_init = true;  // the populations are what lbm_init made
     size_t base_bytes = 0;      // device bytes lbm_init allocated
     lbm_adjoint_state adj;

@@ -51,6 +51,8 @@ def _init(libonly, **kw):
     (dict(adjoint_steps=3), "adjoint_steps"),
     (dict(adjoint_steps=-1), "adjoint_steps"),
     (dict(adjoint_max_states=-2), "adjoint_max_states"),
+    (dict(graph_iterations=3), "graph_iterations"),
+    (dict(graph_iterations=512), "graph_iterations"),
 ])
 def test_init_rejects_bad_arguments(libonly, kw, frag):
     rc, msg = _init(libonly, **kw)
