@@ -254,3 +254,19 @@ def test_graph_replay_matches_direct_launches(capi, prec, nsteps, every):
     for r in res[1:]:
         for a, b in zip(res[0], r):
             np.testing.assert_array_equal(a.view(np.uint8), b.view(np.uint8))
+
+
+@pytest.mark.parametrize("prec,kernel", [("fp32", "direct"), ("fp32", "staged"), ("fp16", "narrow"),
+                                         ("fp16", "staged"), ("bf16", "direct")])
+def test_graph_replay_every_kernel_variant(capi, prec, kernel):
+    """Graph replay of each iteration-kernel variant (the staged one with its
+    mbarrier ring and dynamic shared memory) equals its direct launches."""
+    res = []
+    for g in (0, 1):
+        with capi.Lattice(48, 0.0089, 0.05, precision=prec, stride=0, seed=4, noise_sigma=1e-4, kernel=kernel,
+                          graph_iterations=g) as L:
+            L.step(3)
+            L.step(40, every=40)
+            res.append((L.f(), L.rho(), L.u()))
+    for a, b in zip(*res):
+        np.testing.assert_array_equal(a.view(np.uint8), b.view(np.uint8))
