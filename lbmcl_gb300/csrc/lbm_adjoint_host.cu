@@ -414,14 +414,21 @@ int lbm_adjoint_forward(lbm_t *h, int iterations, int checkpoint_every, double *
     s.every = c;
     s.init_state = h->state_is_init;
 
-    // Q_0, then the iterations, copying Q_{jc} into checkpoint j
+    // Q_0, then the iterations, copying Q_{jc} into checkpoint j; runs that
+    // stay inside one checkpoint interval replay the step graph
     ADJ_CUDA(cudaMemcpyAsync(s.ckpt[0], h->f[h->cur], fbytes, cudaMemcpyDeviceToDevice, h->stream));
-    for (int k = 0; k < iterations; ++k) {
-        ADJ_CUDA(lbm::launch_iteration(h, h->f[h->cur], h->f[h->cur ^ 1]));
-        h->cur ^= 1;
-        const int done = k + 1;
-        if (done < iterations && done % c == 0)
-            ADJ_CUDA(cudaMemcpyAsync(s.ckpt[done / c], h->f[h->cur], fbytes, cudaMemcpyDeviceToDevice, h->stream));
+    for (int k = 0; k < iterations;) {
+        const int G = h->graph_iters, next_ck = (k / c + 1) * c;
+        if (G > 1 && k + G <= iterations && k + G <= next_ck) {
+            ADJ_CUDA(lbm::replay_iterations(h));
+            k += G;
+        } else {
+            ADJ_CUDA(lbm::launch_iteration(h, h->f[h->cur], h->f[h->cur ^ 1]));
+            h->cur ^= 1;
+            ++k;
+        }
+        if (k < iterations && k % c == 0)
+            ADJ_CUDA(cudaMemcpyAsync(s.ckpt[k / c], h->f[h->cur], fbytes, cudaMemcpyDeviceToDevice, h->stream));
     }
     h->it += iterations;
     h->state_is_init = false;

@@ -98,6 +98,9 @@ inline size_t storage_bytes(int prec) { return prec == LBM_FP64 ? 8 : (prec == L
 inline size_t macro_bytes(int prec) { return prec == LBM_FP64 ? 8 : 4; }
 // launch one iteration P_out = C(S(P_in)) with the handle's kernel variant
 cudaError_t launch_iteration(const lbm_t *h, const void *fin, void *fout);
+// h->graph_iters iterations from h->f[h->cur] as one replayed CUDA graph
+// (an even count: h->cur is unchanged)
+cudaError_t replay_iterations(lbm_t *h);
 // free the device memory of an adjoint state
 void release_adjoint(lbm_t *h);
 }  // namespace lbm
