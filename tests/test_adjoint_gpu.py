@@ -211,3 +211,38 @@ def test_adjoint_matches_reference_adjoint(capi, prec, dim, iters):
     assert bad.size == 0, f"{len(bad)} slots differ, first (q, z, y, x) = {bad[:5].tolist()}"
     assert np.abs(gl - gl_ref).max() <= tol * np.abs(gl_ref).max()
     assert abs(gt - gt_ref) <= tol * abs(gt_ref)
+
+
+def test_adjoint_api_errors(capi):
+    """Misuse of the gradient entry points returns a status and a message
+    (no exit, no CUDA error), and leaves the handle usable."""
+    import ctypes as C
+    dim = 16
+    lid, target = setup_case(dim, 21)
+    L = capi.lib()
+    with capi.Lattice(dim, velocity=0.0, precision="fp32", lid=lid, tau=0.53) as lat:
+        h = lat.h
+        # the loss plane must hold FLUID sites
+        for bad in (0, 1, dim - 2, dim):
+            assert L.lbm_adjoint_set_loss(h, bad, None) == capi.EINVAL
+        # a forward needs a loss; a backward needs the forward of the current state
+        J = C.c_double()
+        assert L.lbm_adjoint_forward(h, 5, 5, C.byref(J)) == capi.ESTATE
+        gt = C.c_double()
+        assert L.lbm_adjoint_backward(h, 1.0, C.byref(gt), None, None, 0) == capi.ESTATE
+        lat.adjoint_set_loss(8, target)
+        assert L.lbm_adjoint_forward(h, 0, 5, C.byref(J)) == capi.EINVAL
+        assert L.lbm_adjoint_forward(h, 5, 0, C.byref(J)) == capi.EINVAL
+        lat.adjoint_forward(6, 3)
+        # a gradient buffer of the wrong size
+        buf = np.zeros(10, np.float32)
+        assert L.lbm_adjoint_backward(h, 1.0, C.byref(gt), None, buf.ctypes.data_as(C.c_void_p), buf.nbytes) \
+            == capi.EINVAL
+        assert "grad_f0" in L.lbm_last_error().decode()
+        # stepping after the forward invalidates it
+        lat.step(1)
+        assert L.lbm_adjoint_backward(h, 1.0, C.byref(gt), None, None, 0) == capi.ESTATE
+        # and the handle still works
+        J2 = lat.adjoint_forward(6, 3)
+        g = lat.adjoint_backward(1.0, want_f0=False)
+        assert np.isfinite(J2) and np.isfinite(g[0]) and np.isfinite(g[1]).all()
