@@ -516,7 +516,12 @@ int lbm_adjoint_backward(lbm_t *h, double dloss, double *grad_tau, double *grad_
         size_t freeb = 0, totalb = 0;
         ADJ_CUDA(cudaMemGetInfo(&freeb, &totalb));
         const size_t margin = ((size_t)1 << 30) + totalb / 50;  // for the runtime and other users
-        const size_t fit = freeb > margin ? (freeb - margin) / fbytes : 0;
+        size_t fit = freeb > margin ? (freeb - margin) / fbytes : 0;
+        const size_t cap = h->cfg.max_device_bytes;  // the handle's budget, if any
+        if (cap > 0) {
+            const size_t used = h->base_bytes + h->adj.bytes;
+            fit = std::min(fit, cap > used ? (cap - used) / fbytes : (size_t)0);
+        }
         size_t want_total = (size_t)(c - 1);
         if (h->cfg.adjoint_max_states > 0) want_total = std::min(want_total, (size_t)h->cfg.adjoint_max_states);
         if (want_total > s.seg.size() + fit) {
@@ -530,7 +535,8 @@ int lbm_adjoint_backward(lbm_t *h, double dloss, double *grad_tau, double *grad_
             want_total > s.seg.size() ? (int)std::min<size_t>(want_total - s.seg.size(), fit) : 0;
         for (int k = 0; k < want; ++k) {
             void *p = nullptr;
-            if (alloc_tracked(h, &p, fbytes) != LBM_OK) break;  // budget reached: recurse with fewer
+            const int rc = alloc_tracked(h, &p, fbytes);
+            if (rc != LBM_OK) return rc;
             s.seg.push_back(p);
         }
     }
