@@ -137,13 +137,23 @@ bool two_step(const lbm_t *h)
 template <class S>
 cudaError_t run_adjoint2(const lbm::Adj2Args &a, unsigned grid, cudaStream_t s)
 {
-    // set on every launch: the attribute belongs to the current device's
-    // context, and handles may live on different devices and threads
-    const cudaError_t e = cudaFuncSetAttribute(lbm::adjoint2_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                               (int)lbm::ADJ2_SMEM);
-    if (e != cudaSuccess) return e;
     lbm::adjoint2_kernel<S><<<grid, lbm::ADJ2_EX * lbm::ADJ2_EY, lbm::ADJ2_SMEM, s>>>(a);
     return cudaGetLastError();
+}
+
+// The two-step kernel's shared-memory size, set at the start of every
+// backward sweep (outside any graph capture): the attribute belongs to the
+// current device's context, and handles may live on different devices.
+cudaError_t prepare_adjoint2(const lbm_t *h)
+{
+    const int bytes = (int)lbm::ADJ2_SMEM;
+    const cudaFuncAttribute at = cudaFuncAttributeMaxDynamicSharedMemorySize;
+    switch (h->prec) {
+    case LBM_FP32: return cudaFuncSetAttribute(lbm::adjoint2_kernel<float>, at, bytes);
+    case LBM_FP16: return cudaFuncSetAttribute(lbm::adjoint2_kernel<__half>, at, bytes);
+    case LBM_BF16: return cudaFuncSetAttribute(lbm::adjoint2_kernel<__nv_bfloat16>, at, bytes);
+    default: return cudaSuccess;
+    }
 }
 
 // a_{k+1} -> a_{k-1} with Q_k (fwd_a) and Q_{k-1} (fwd_b)
@@ -227,6 +237,13 @@ int alloc_tracked(lbm_t *h, void **p, size_t bytes)
     ADJ_CUDA(cudaMalloc(p, bytes));
     h->adj.bytes += bytes;
     return LBM_OK;
+}
+
+void drop_segment_graphs(lbm_adjoint_state &s)
+{
+    for (cudaGraphExec_t &g : s.seg_exec)
+        if (g) cudaGraphExecDestroy(g), g = nullptr;
+    s.seg_graph_c = 0;
 }
 
 void free_tracked(lbm_t *h, void *p, size_t bytes)
@@ -335,6 +352,42 @@ int sweep(lbm_t *h, const void *q0, int start, int len, const std::vector<void *
     return LBM_OK;
 }
 
+// One full segment of the one-level sweep (c - 1 recomputed iterations
+// from the staged first state s.q0, then its c adjoint steps) as a captured
+// CUDA graph, replayed for every full segment: the launches of a launch-bound
+// small lattice cost one graph launch.  One graph per adjoint-buffer parity.
+int replay_segment(lbm_t *h, int c, int &cur)
+{
+    lbm_adjoint_state &s = h->adj;
+    cudaGraphExec_t &exec = s.seg_exec[cur];
+    if (!exec) {
+        ADJ_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+        int c2 = cur, rc = LBM_OK;
+        for (int m = 1; m < c && rc == LBM_OK; ++m) {
+            const cudaError_t e = lbm::launch_iteration(h, m == 1 ? s.q0 : s.seg[m - 2], s.seg[m - 1]);
+            if (e != cudaSuccess) rc = fail(LBM_ECUDA, "segment capture: %s", cudaGetErrorString(e));
+        }
+        if (rc == LBM_OK)
+            rc = adjoint_steps_down(h, 0, c, [&](int k) -> const void * { return k == 0 ? s.q0 : s.seg[k - 1]; }, c2);
+        cudaGraph_t g = nullptr;
+        const cudaError_t ec = cudaStreamEndCapture(h->stream, &g);
+        if (rc == LBM_OK && ec != cudaSuccess) rc = fail(LBM_ECUDA, "segment capture: %s", cudaGetErrorString(ec));
+        if (rc == LBM_OK) {
+            const cudaError_t ei = cudaGraphInstantiate(&exec, g, 0);
+            if (ei != cudaSuccess) {
+                exec = nullptr;
+                rc = fail(LBM_ECUDA, "segment graph: %s", cudaGetErrorString(ei));
+            }
+        }
+        if (g) cudaGraphDestroy(g);
+        if (rc != LBM_OK) return rc;
+        s.seg_flip[cur] = c2 ^ cur;
+    }
+    ADJ_CUDA(cudaGraphLaunch(exec, h->stream));
+    cur ^= s.seg_flip[cur];
+    return LBM_OK;
+}
+
 }  // namespace
 
 namespace lbm {
@@ -349,8 +402,10 @@ void release_adjoint(lbm_t *h)
         if (p) cudaFree(p);
         p = nullptr;
     }
-    for (void *p : {(void *)s.grad_lid, (void *)s.tau_acc, (void *)s.loss_part, s.target})
+    for (void *p : {(void *)s.grad_lid, (void *)s.tau_acc, (void *)s.loss_part, s.target, s.q0})
         if (p) cudaFree(p);
+    s.q0 = nullptr;
+    drop_segment_graphs(s);
     s.grad_lid = nullptr;
     s.tau_acc = nullptr;
     s.loss_part = nullptr;
@@ -396,11 +451,13 @@ int lbm_adjoint_forward(lbm_t *h, int iterations, int checkpoint_every, double *
     if (h->adj.plane_y < 0) return fail(LBM_ESTATE, "lbm_adjoint_forward: call lbm_adjoint_set_loss first");
     lbm_adjoint_state &s = h->adj;
     const size_t fbytes = (size_t)lbm::Q * h->n * lbm::storage_bytes(h->prec);
-    // drop the previous run's state buffers (the target and work buffers stay)
+    // drop the previous run's state buffers (the target and work buffers
+    // stay) and the segment graphs that point at them
     for (void *p : s.ckpt) free_tracked(h, p, fbytes);
     for (void *p : s.seg) free_tracked(h, p, fbytes);
     s.ckpt.clear();
     s.seg.clear();
+    drop_segment_graphs(s);
     s.ready = false;
     const int c = std::min(checkpoint_every, iterations);
     const int nck = (iterations + c - 1) / c;
@@ -485,6 +542,7 @@ int lbm_adjoint_backward(lbm_t *h, double dloss, double *grad_tau, double *grad_
     if (s.tau_acc && s.adj_grid != agrid) {
         free_tracked(h, s.tau_acc, (size_t)s.adj_grid * sizeof(double));
         s.tau_acc = nullptr;
+        drop_segment_graphs(s);
     }
     if (!s.tau_acc) {
         int rc = alloc_tracked(h, (void **)&s.tau_acc, (size_t)agrid * sizeof(double));
@@ -540,10 +598,32 @@ int lbm_adjoint_backward(lbm_t *h, double dloss, double *grad_tau, double *grad_
             s.seg.push_back(p);
         }
     }
-    // segments, last to first
+    // segments, last to first.  Full segments of the one-level sweep replay
+    // a captured graph from a staged copy of their checkpoint (one state copy
+    // per segment) when graphs are on and the copy buffer fits.
+    ADJ_CUDA(prepare_adjoint2(h));
     const int nck = (T + c - 1) / c;
+    bool graphs = h->graph_iters > 1 && c >= 2 && (int)s.seg.size() >= c - 1;
+    if (graphs && s.seg_graph_c != c) {  // graphs of another segment length
+        drop_segment_graphs(s);
+        s.seg_graph_c = c;
+    }
+    if (graphs && !s.q0) {
+        size_t freeb = 0, totalb = 0;
+        ADJ_CUDA(cudaMemGetInfo(&freeb, &totalb));
+        const size_t cap = h->cfg.max_device_bytes;
+        const bool fits = freeb > fbytes + ((size_t)1 << 30) &&
+                          (cap == 0 || h->base_bytes + s.bytes + fbytes <= cap);
+        if (!fits || alloc_tracked(h, &s.q0, fbytes) != LBM_OK) graphs = false;
+    }
     for (int j = nck - 1; j >= 0; --j) {
         const int start = j * c, len = std::min(T, start + c) - start;
+        if (graphs && len == c) {
+            ADJ_CUDA(cudaMemcpyAsync(s.q0, s.ckpt[j], fbytes, cudaMemcpyDeviceToDevice, st));
+            const int rc = replay_segment(h, c, cur);
+            if (rc != LBM_OK) return rc;
+            continue;
+        }
         const int rc = sweep(h, s.ckpt[j], start, len, s.seg, 0, (int)s.seg.size(), cur);
         if (rc != LBM_OK) return rc;
     }

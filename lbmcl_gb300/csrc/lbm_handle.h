@@ -28,6 +28,12 @@ struct lbm_adjoint_state {
     bool ready = false;        // a forward was recorded and Q_T is current
     int64_t it_end = -1;       // handle iteration count when the forward ended
     size_t bytes = 0;          // device bytes held by this state
+    // graph replay of full segments: the staged first state, one graph per
+    // adjoint-buffer parity, the parity flip of one segment, its length
+    void *q0 = nullptr;
+    cudaGraphExec_t seg_exec[2] = {nullptr, nullptr};
+    int seg_flip[2] = {0, 0};
+    int seg_graph_c = 0;
 };
 
 struct lbm_handle {

@@ -246,3 +246,30 @@ def test_adjoint_api_errors(capi):
         J2 = lat.adjoint_forward(6, 3)
         g = lat.adjoint_backward(1.0, want_f0=False)
         assert np.isfinite(J2) and np.isfinite(g[0]) and np.isfinite(g[1]).all()
+
+
+@pytest.mark.parametrize("prec,steps,every", [("fp32", 1, 8), ("fp32", 2, 10), ("fp16", 2, 6), ("fp64", 1, 5)])
+def test_segment_graph_replay_is_exact(capi, prec, steps, every):
+    """Full segments of the backward sweep replayed as one captured graph
+    (from a staged copy of the checkpoint) against direct launches: the
+    same launches on the same states, bit for bit; a second sweep reuses the
+    graphs."""
+    dim, iters = 24, 43
+    lid, target = setup_case(dim, 17)
+    res = []
+    for g in (0, 1):
+        with capi.Lattice(dim, velocity=0.0, precision=prec, lid=lid, tau=0.53, seed=6, noise_sigma=1e-4,
+                          adjoint_steps=steps, graph_iterations=g) as L:
+            L.adjoint_set_loss(12, target)
+            f0 = L.f()
+            out = []
+            for _ in range(2):  # the same start each time (the forward advances the state)
+                L.load_f(f0)
+                J = L.adjoint_forward(iters, every)
+                out.append((J,) + tuple(L.adjoint_backward(1.0)))
+            res.append(out)
+    for a, b in zip(res[0], res[1]):
+        assert a[0] == b[0] and a[1] == b[1]
+        np.testing.assert_array_equal(a[2], b[2])
+        np.testing.assert_array_equal(a[3], b[3])
+    assert res[0][0][1] == res[0][1][1]   # the replayed second sweep repeats the first
