@@ -1,6 +1,7 @@
 """The C-ABI library without a GPU: it loads, exports every function
 include/lbm.h declares, and rejects bad arguments before touching CUDA."""
 import ctypes as C
+import os
 import subprocess
 
 import pytest
@@ -85,3 +86,17 @@ def test_lid_profile_must_be_finite(libonly):
     lid[7] = np.nan
     rc, msg = _init(libonly, lid_profile=lid.ctypes.data_as(C.POINTER(C.c_double)))
     assert rc == libonly.EINVAL and "lid_profile" in msg
+
+
+def test_header_is_plain_c(tmp_path):
+    """include/lbm.h compiles as C99 (callers bind it from C, cgo, JNI ...)."""
+    import shutil
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+    src = tmp_path / "use.c"
+    src.write_text('#include "lbm.h"\nint main(void) { lbm_config c; lbm_config_default(&c); return c.dim; }\n')
+    r = subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I" + inc, "-fsyntax-only",
+                        str(src)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
