@@ -9,12 +9,18 @@ iteration over the whole lattice.  The headline value is the FP16-deviation
 storage kernel (nu = 0.005, lid u = 0.08, N(0, 1e-4) seeded noise); BF16,
 FP32 and FP64 are measured in the same run and reported under "modes".
 
-Timing: W untimed iterations, then K iterations bracketed by CUDA events
-recorded on the library's own stream, with a device synchronisation (and, for
-N > 1, a barrier) on both sides; the max over ranks is reported.  Each
+Timing: W untimed iterations, then windows of exactly K iterations, each
+bracketed by CUDA events recorded on the library's own stream, with a device
+synchronisation (and, for N > 1, a barrier) on both sides of the timed
+region; the headline mode runs at least --repeats windows and at least one
+second of them, and reports the median window (so the clock record has
+samples under load even for small K); the max over ranks is reported.  Each
 lattice is 10-41 GB, far larger than the 129 MB L2, so no L2 flush is needed
 between iterations.  SM clocks are sampled with nvidia-smi during the timed
 region.
+
+A 256^3 block (the plain-precision cavity: nu = 0.0089, lid 0.05, seeded
+noise) reports FP32 and FP64 MLUPS and %HBM with the CPU path at 256^3.
 
 --impl reference times the reference algorithm on the host CPU instead (the
 oracle's C restatement of kernels.cl with OpenMP on all host threads; the
@@ -131,31 +137,44 @@ def _events():
     return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
 
-def time_mode(capi, prec, steps, warmup, device, barrier=None, sampler=None):
-    """Device-resident iterations of one storage mode; returns ms per step."""
+def time_mode(capi, prec, steps, warmup, device, barrier=None, sampler=None, repeats=1, workload=None,
+              min_window_s=0.0):
+    """Device-resident iterations of one storage mode: `warmup` untimed
+    iterations, then `repeats` back-to-back windows of exactly `steps`
+    iterations, each bracketed by CUDA events on the library's stream (and
+    more windows while their total stays under min_window_s, so that the
+    clock sampler sees the GPU under load); returns (median ms per step,
+    every window's ms per step)."""
     import torch
-    dim = WORKLOAD["dim"]
-    with capi.Lattice(dim, WORKLOAD["viscosity"], WORKLOAD["velocity"], precision=prec, stride=0,
-                      seed=WORKLOAD["seed"], noise_sigma=WORKLOAD["noise_sigma"], device=device) as L:
+    w = dict(WORKLOAD if workload is None else workload)
+    dim = w["dim"]
+    with capi.Lattice(dim, w["viscosity"], w["velocity"], precision=prec, stride=0,
+                      seed=w["seed"], noise_sigma=w["noise_sigma"], device=device) as L:
         stream = torch.cuda.ExternalStream(L.stream, device=device)
         L.step(warmup)
         L.sync()
-        e0, e1 = _events()
         if barrier:
             barrier()
         torch.cuda.synchronize(device)
         ctx = sampler if sampler is not None else _Null()
+        windows = []
         with ctx:
-            e0.record(stream)
-            L.step(steps)
-            e1.record(stream)
-            e1.synchronize()
+            total = 0.0
+            while len(windows) < repeats or total < min_window_s * 1e3:
+                e0, e1 = _events()
+                e0.record(stream)
+                L.step(steps)
+                e1.record(stream)
+                e1.synchronize()
+                windows.append(e0.elapsed_time(e1) / steps)
+                total += windows[-1] * steps
+                if len(windows) >= 1000:
+                    break
         torch.cuda.synchronize(device)
         if barrier:
             barrier()
-        ms = e0.elapsed_time(e1)
         L.sync()  # raises if the run diverged
-        return ms / steps
+        return float(np.median(windows)), windows
 
 
 class _Null:
@@ -286,13 +305,14 @@ def trimmed_mean(values):
     return sum(v[1:-1]) / (len(v) - 2)
 
 
-def cpu_oracle_mlups(budget_s, dim=512, threads=0, runs=10):
-    """Oracle push step (FP32, all host threads) over z-slabs of a dim^3
-    lattice, `runs` timed slabs and their trimmed mean (as benchmark.sh
-    aggregates its runs); returns (MLUPS, threads, description, seconds)."""
+def cpu_oracle_mlups(budget_s, dim=512, threads=0, runs=10, precision="f32", workload=None):
+    """Oracle push step (all host threads) over z-slabs of a dim^3 lattice,
+    `runs` timed slabs and their trimmed mean (as benchmark.sh aggregates its
+    runs); returns (MLUPS, threads, description, seconds)."""
     from oracle import pyoracle as po
     po.build()
-    L = po.OracleLattice(dim, WORKLOAD["viscosity"], WORKLOAD["velocity"], "f32", stride=None, threads=threads)
+    w = WORKLOAD if workload is None else workload
+    L = po.OracleLattice(dim, w["viscosity"], w["velocity"], precision, stride=None, threads=threads)
     nthreads = threads or po.lib().lbmo_max_threads()
     # calibrate on 8 planes
     t = time.perf_counter()
@@ -306,8 +326,9 @@ def cpu_oracle_mlups(budget_s, dim=512, threads=0, runs=10):
         times.append(time.perf_counter() - t)
     secs = trimmed_mean(times)
     sites = planes * dim * dim
-    desc = (f"oracle C restatement of kernels.cl, FP32, OpenMP {nthreads} threads, {planes} z-planes "
-            f"({sites / 1e6:.1f} M site updates) of a {dim}^3 lattice per run, trimmed mean of {runs} runs")
+    desc = (f"oracle C restatement of kernels.cl, {'FP32' if precision == 'f32' else 'FP64'}, OpenMP {nthreads} "
+            f"threads, {planes} z-planes ({sites / 1e6:.1f} M site updates) of a {dim}^3 lattice per run, "
+            f"trimmed mean of {runs} runs")
     return sites / secs / 1e6, nthreads, desc, sum(times)
 
 
@@ -357,6 +378,9 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint/forward leg")
+    ap.add_argument("--no-config2", action="store_true", help="skip the 256^3 FP32 / FP64 leg")
+    ap.add_argument("--repeats", type=int, default=5,
+                    help="timed windows of --steps iterations for the headline mode (median reported)")
     ap.add_argument("--modes", default="fp16,bf16,fp32,fp64")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -385,16 +409,43 @@ def main():
     res = {}
     sampler = ClockSampler(device)
     for m in modes:
-        # headline mode: K steps; the others a bounded share of the run
-        k = args.steps if m == modes[0] else (max(10, args.steps // 5) if m != "fp64" else max(5, args.steps // 50))
-        ms = time_mode(capi, m, k, args.warmup if m != "fp64" else 3, device, barrier,
-                       sampler if m == modes[0] else None)
+        # headline mode: windows of K steps, repeated (at least `--repeats`,
+        # and for at least one second so the clock record has samples under
+        # load), median reported; the others one window, a bounded share
+        head_mode = m == modes[0]
+        k = args.steps if head_mode else (max(10, args.steps // 5) if m != "fp64" else max(5, args.steps // 50))
+        ms, wins = time_mode(capi, m, k, args.warmup if m != "fp64" else 3, device, barrier,
+                             sampler if head_mode else None, repeats=args.repeats if head_mode else 1,
+                             min_window_s=1.0 if head_mode else 0.0)
         ms = slowest_rank_ms(ms, ws, f"cuda:{device}")
         mlups = wet / (ms * 1e3)
         gbs = wet * BYTES_PER_SITE[m] / (ms * 1e-3) / 1e9
         res[m] = {"mlups": round(job_mlups(wet, ms, ws), 1), "mlups_per_gpu": round(mlups, 1),
                   "ms_per_step": round(ms, 4),
                   "gbs": round(gbs, 1), "frac_hbm": round(gbs / peak, 4), "steps": k}
+        if head_mode:
+            res[m]["windows"] = len(wins)
+            res[m]["window_ms_per_step_min_max"] = [round(min(wins), 4), round(max(wins), 4)]
+
+    # the plain-precision cavity: 256^3, nu = 0.0089, lid 0.05, seeded noise,
+    # FP32 and FP64 with the CPU path at the same size
+    config2 = None
+    if not args.no_config2:
+        c2 = dict(dim=256, viscosity=0.0089, velocity=0.05, seed=1234, noise_sigma=1e-4)
+        wet2 = (c2["dim"] - 2) ** 3
+        config2 = {"workload": "D3Q19 BGK lid-driven cavity 256^3, nu=0.0089, lid u=0.05, N(0,1e-4) noise seed 1234",
+                   "wet_sites": wet2}
+        for m, k in (("fp32", max(100, args.steps)), ("fp64", max(20, args.steps // 10))):
+            ms, _ = time_mode(capi, m, k, 3, device, barrier, workload=c2)
+            ms = slowest_rank_ms(ms, ws, f"cuda:{device}")
+            gbs = wet2 * BYTES_PER_SITE[m] / (ms * 1e-3) / 1e9
+            config2[m] = {"mlups": round(job_mlups(wet2, ms, ws), 1), "ms_per_step": round(ms, 4),
+                          "gbs": round(gbs, 1), "frac_hbm": round(gbs / peak, 4), "steps": k}
+        if rank == 0 and not args.no_cpu:
+            for m in ("f32", "f64"):
+                v, cores, desc, _ = cpu_oracle_mlups(6.0, dim=c2["dim"], precision=m, workload=c2)
+                config2["cpu_" + m] = {"value": round(v, 3), "unit": "MLUPS", "cores": cores, "kind": "port",
+                                       "sample": desc}
 
     head = modes[0]
     ms_head = res[head]["ms_per_step"]
@@ -427,6 +478,7 @@ def main():
             "ratio_fp16_vs_fp32": round(res["fp16"]["mlups"] / res["fp32"]["mlups"], 3)
             if "fp16" in res and "fp32" in res else None,
             "adjoint": adjoint,
+            "config_256": config2,
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
                          "kernel": "pull_kernel, one iteration = interior-row launch + face-row launch",
@@ -438,7 +490,9 @@ def main():
             "e2e": {"value": round(e2e_mlups, 1), "unit": "MLUPS", "h2d_bytes_per_step": h2d / args.steps,
                     "d2h_bytes_per_step": d2h / args.steps,
                     "what": "lbm_init (host config + lid profile) + K iterations + rho/u read-back to pinned host"},
-            "gpu_launches": 2 * args.steps,
+            "gpu_launches": 2 * args.steps * res[head]["windows"],
+            "timed_windows": {"windows": res[head]["windows"], "steps_per_window": args.steps,
+                              "reported": "median window"},
             "clocks": sampler.summary(),
             "cpu_baseline": cpu,
         }

@@ -211,31 +211,35 @@ const char *lbm_last_error(void);
  * The sums of lbm_reduce (out[0] mass, out[1] kinetic energy, out[2] number
  * of FLUID and MOVING sites) for a lattice state held in the caller's own
  * device memory, computed without allocating anything.  It is meant for
- * callers that cannot call cudaMalloc: code that runs while a CUDA graph is
- * being captured (allocation cannot be captured), and processes whose device
- * memory belongs to another allocator (a framework's caching pool, a fixed
- * arena in a real-time loop) or is fully committed.  Such callers cannot
- * create a handle (lbm_init allocates) but can pass pointers to buffers they
- * own.
+ * callers that cannot call cudaMalloc: processes whose device memory belongs
+ * to another allocator (a framework's caching pool, a fixed arena sized once
+ * at start-up in a real-time loop), or whose device memory is already fully
+ * committed, so that a further cudaMalloc would fail or would bypass the
+ * owner's accounting.  Such callers cannot create a handle (lbm_init
+ * allocates) but can pass pointers to buffers they own.
  *
  *   f      the populations in the LBM_DUMP_F_RAW layout of `precision`
  *          (19 planes of dim^3 storage elements; the post-collision state
- *          a handle holds after its last iteration)
- *   map    the byte map (LBM_DUMP_MAP_U8), dim^3 bytes
+ *          a handle holds after its last iteration); 16-byte aligned
+ *   map    the byte map (LBM_DUMP_MAP_U8), dim^3 bytes; aligned to 16 /
+ *          (storage element size) bytes (4 for FP32, 2 for FP64, 8 for
+ *          FP16 / BF16)
  *   lid    the lid u_x of each column, dim*dim values of the macro type
- *          (double for LBM_FP64, float otherwise)
+ *          (double for LBM_FP64, float otherwise), aligned to that type
  *   stream cudaStream_t to run on (NULL: the legacy default stream); the call
  *          returns after the stream has finished the reduction
- * All three buffers must be on the calling thread's current device.
+ * All three buffers must be on the calling thread's current device.  A
+ * misaligned pointer is rejected with LBM_EINVAL before anything runs.
  *
  * The block partial sums live in one fixed __device__ array of
  * LBM_NOALLOC_SCRATCH_BYTES (32 KiB + 32 B) that every GPU which loads the
  * library holds until the process exits; a launch uses at most
  * LBM_NOALLOC_MAX_BLOCKS blocks per row kind so the partials always fit, and
  * dim is limited to LBM_NOALLOC_MAX_DIM (larger: LBM_EINVAL).  The first call
- * on a device looks up that array's device address (cudaGetSymbolAddress) with
- * the device current; make that first call before any stream capture.  Every
- * call reuses the same array, which keeps the last call's contents (the
+ * on a device looks up that array's device address (cudaGetSymbolAddress)
+ * with the device current and keeps it for the life of the process, so the
+ * entry point must not be used on a device after cudaDeviceReset there.
+ * Every call reuses the same array, which keeps the last call's contents (the
  * status word is cleared at the start of each call), so calls that overlap on
  * the GPU -- on different streams, or from several host threads -- race and
  * must be serialised by the caller.  Returns LBM_EDIVERGED (with out filled)

@@ -439,6 +439,10 @@ int lbm_adjoint_set_loss(lbm_t *h, int plane_y, const double *target_ux)
     ADJ_CUDA(cudaMemcpyAsync(h->adj.target, buf.data(), buf.size(), cudaMemcpyHostToDevice, h->stream));
     ADJ_CUDA(cudaStreamSynchronize(h->stream));
     h->adj.plane_y = plane_y;
+    // a new loss invalidates the recorded forward (its loss value belongs to
+    // the old plane / target) and the captured segment graphs with it
+    drop_segment_graphs(h->adj);
+    h->adj.ready = false;
     return LBM_OK;
 }
 

@@ -2,11 +2,12 @@
 // state that lives in the caller's own device memory, computed without any
 // device allocation.
 //
-// Why: some callers cannot call cudaMalloc -- code running while a CUDA graph
-// is being captured (allocation is not capturable), processes whose device
-// memory is owned by another allocator (a framework's caching pool, a fixed
-// arena in a real-time loop) or that have already committed all memory.  They
-// can still hand this library device pointers to buffers they own.
+// Why: some callers cannot call cudaMalloc -- processes whose device memory
+// is owned by another allocator (a framework's caching pool, a fixed arena
+// sized once at start-up in a real-time loop) or that have already committed
+// all of it, so a further cudaMalloc would fail or escape the owner's
+// accounting.  They can still hand this library device pointers to buffers
+// they own.
 //
 // How: the block partial sums that lbm_reduce keeps in a handle-owned buffer
 // live here in one file-scope __device__ array of fixed size, which every GPU
@@ -15,9 +16,11 @@
 // partials always fit.  On the first call on a device, with that device
 // current, the host looks up the array's device address once with
 // cudaGetSymbolAddress and passes it to the kernels; the host-side symbol is
-// only a stand-in and is never handed to a kernel.
+// only a stand-in and is never handed to a kernel.  The address is kept for
+// the life of the process (a cudaDeviceReset would invalidate it).
 #include <algorithm>
 #include <cstdarg>
+#include <cstdint>
 #include <cstdio>
 #include <mutex>
 
@@ -141,6 +144,15 @@ extern "C" int lbm_reduce_noalloc(const void *f, const uint8_t *map, const void 
         return fail(LBM_EINVAL,
                     "lbm_reduce_noalloc: dim %d must be in [4, %d] and a multiple of %d for this precision", dim,
                     LBM_NOALLOC_MAX_DIM, mult);
+    // the kernels read f with 16-byte vectors, the map in words of one byte
+    // per site of a vector, the lid as the macro type: a misaligned pointer
+    // (an offset view into a pool) would fault the caller's context
+    const size_t sb = precision == LBM_FP64 ? 8 : (precision == LBM_FP32 ? 4 : 2);
+    const size_t map_align = 16 / sb, lid_align = precision == LBM_FP64 ? 8 : 4;
+    if ((uintptr_t)f % 16 != 0 || (uintptr_t)map % map_align != 0 || (uintptr_t)lid % lid_align != 0)
+        return fail(LBM_EINVAL,
+                    "lbm_reduce_noalloc: misaligned buffer (f needs 16-byte, map %zu-byte, lid %zu-byte alignment)",
+                    map_align, lid_align);
 
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -162,7 +174,6 @@ extern "C" int lbm_reduce_noalloc(const void *f, const uint8_t *map, const void 
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     int *status = reinterpret_cast<int *>(scratch + kStatusSlot);
 
-    const size_t sb = precision == LBM_FP64 ? 8 : (precision == LBM_FP32 ? 4 : 2);
     lbm::StepArgs a = {};
     a.fin = f;
     a.fout = nullptr;

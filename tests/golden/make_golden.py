@@ -73,7 +73,8 @@ def run_digests(name, spec, lids):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference", help="path of the reference checkout")
+    ap.add_argument("--ref", default=os.environ.get("LBMCL_REF", "/root/reference"),
+                    help="path of the reference checkout (default: $LBMCL_REF)")
     args = ap.parse_args()
     if not po.ref_available("f32") or not po.ref_available("f64"):
         sys.exit("oracle/_ref is not built: run `make -C oracle ref REF=<path>` first")

@@ -100,3 +100,23 @@ def test_header_is_plain_c(tmp_path):
     r = subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I" + inc, "-fsyntax-only",
                         str(src)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+@pytest.mark.parametrize("which", ["f", "map", "lid", "dim"])
+def test_noalloc_checks_arguments_before_cuda(libonly, which):
+    """lbm_reduce_noalloc refuses misaligned buffers and oversized lattices on
+    the host, before any CUDA call (nothing is dereferenced)."""
+    L = libonly.lib()
+    fn = L.lbm_reduce_noalloc
+    fn.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.POINTER(C.c_double)]
+    fn.restype = C.c_int
+    ptrs = {"f": 1 << 20, "map": 1 << 20, "lid": 1 << 20}
+    dim = 32
+    if which == "dim":
+        dim = 4096
+    else:
+        ptrs[which] += 1 if which == "map" else 2
+    out = (C.c_double * 3)()
+    rc = fn(C.c_void_p(ptrs["f"]), C.c_void_p(ptrs["map"]), C.c_void_p(ptrs["lid"]), dim, libonly.FP32, None, out)
+    assert rc == libonly.EINVAL
+    assert ("dim 4096" if which == "dim" else "misaligned") in L.lbm_last_error().decode()

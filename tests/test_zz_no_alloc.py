@@ -1,8 +1,9 @@
 """lbm_reduce_noalloc: the reduction for callers that cannot allocate device
-memory (graph capture, memory owned by another allocator).  It must give
-what lbm_reduce gives for the same state, call after call, while the only
+memory (device memory owned by another allocator, such as a framework's
+caching pool or a fixed arena, or already fully committed).  It must give
+what lbm_reduce gives for the same state, call after call, and the only
 device memory it touches besides the caller's buffers is its fixed static
-scratch array.
+scratch array: device free memory stays the same across calls.
 
 Collected last on purpose (file name), so a run that stops at the first
 failure has run every other test first.
@@ -42,7 +43,13 @@ def test_noalloc_reduce_matches_lbm_reduce(capi, prec, dim):
     m_d = torch.from_numpy(cmap).to(dev)
     lid_d = torch.tensor(lid, dtype=torch.float64 if prec == "fp64" else torch.float32, device=dev)
     torch.cuda.synchronize()
-    for call in range(2):
+    free_before = None
+    for call in range(4):
+        if call == 1:
+            # the first call may load the library's device code (lazy module
+            # loading); from the second call on, nothing may be allocated
+            torch.cuda.synchronize()
+            free_before = torch.cuda.mem_get_info(dev)[0]
         out = (C.c_double * 3)()
         rc = fn(f_d.data_ptr(), m_d.data_ptr(), lid_d.data_ptr(), dim, capi.PRECISIONS[prec], None, out)
         assert rc == capi.OK, capi.lib().lbm_last_error().decode()
@@ -51,13 +58,29 @@ def test_noalloc_reduce_matches_lbm_reduce(capi, prec, dim):
         assert abs(out[0] - want[0]) <= 1e-12 * abs(want[0]), (call, out[0], want[0])
         assert abs(out[1] - want[1]) <= 1e-9 * abs(want[1]), (call, out[1], want[1])
         assert out[2] == want[2]
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info(dev)[0] == free_before, "device free memory changed across calls"
 
 
 def test_noalloc_rejects_sizes_beyond_its_maximum(capi):
     fn = _noalloc(capi)
     out = (C.c_double * 3)()
-    dummy = C.c_void_p(1)  # never dereferenced: the size check comes first
+    dummy = C.c_void_p(1 << 20)  # never dereferenced: the argument checks come first
     rc = fn(dummy, dummy, dummy, 4096, capi.FP32, None, out)
     assert rc == capi.EINVAL
     assert "dim 4096" in capi.lib().lbm_last_error().decode()
     assert fn(None, dummy, dummy, 32, capi.FP32, None, out) == capi.EINVAL
+
+
+@pytest.mark.parametrize("which", ["f", "map", "lid"])
+def test_noalloc_rejects_misaligned_buffers(capi, which):
+    """A view at an odd offset into a caller's pool is refused on the host,
+    before any launch (nothing is dereferenced)."""
+    fn = _noalloc(capi)
+    out = (C.c_double * 3)()
+    base = 1 << 20
+    ptrs = {"f": base, "map": base, "lid": base}
+    ptrs[which] += 2 if which != "map" else 1
+    rc = fn(C.c_void_p(ptrs["f"]), C.c_void_p(ptrs["map"]), C.c_void_p(ptrs["lid"]), 32, capi.FP32, None, out)
+    assert rc == capi.EINVAL
+    assert "misaligned" in capi.lib().lbm_last_error().decode()
