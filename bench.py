@@ -189,7 +189,8 @@ def time_e2e(capi, prec, steps, device):
     """Through the public API with host buffers: init from the host
     configuration (lid profile copied in), `steps` iterations, and the
     read-back of rho and u into pinned host memory, all inside the timed
-    region (host wall clock around a synchronised sequence)."""
+    region (host wall clock around a synchronised sequence, stopped once the
+    result is in host memory)."""
     import torch
     dim = WORKLOAD["dim"]
     n = dim ** 3
@@ -200,13 +201,18 @@ def time_e2e(capi, prec, steps, device):
     u_h = torch.empty(3 * n, dtype=tdt, pin_memory=True)
     torch.cuda.synchronize(device)
     t0 = time.perf_counter()
-    with capi.Lattice(dim, WORKLOAD["viscosity"], WORKLOAD["velocity"], precision=prec, stride=0, lid=lid,
-                      seed=WORKLOAD["seed"], noise_sigma=WORKLOAD["noise_sigma"], device=device) as L:
+    L = capi.Lattice(dim, WORKLOAD["viscosity"], WORKLOAD["velocity"], precision=prec, stride=0, lid=lid,
+                     seed=WORKLOAD["seed"], noise_sigma=WORKLOAD["noise_sigma"], device=device)
+    try:
         L.step(steps, every=steps)
         L.rho(out=rho_h.numpy())
         L.u(out=u_h.numpy())
         L.sync()
-    t1 = time.perf_counter()
+        # the result is in host memory: the clock stops before the handle's
+        # device memory is released
+        t1 = time.perf_counter()
+    finally:
+        L.close()
     centre = (dim // 2) * (1 + dim + dim * dim)
     assert np.isfinite(rho_h.numpy()[centre]), "e2e run produced a non-finite centre density"
     h2d = lid.nbytes
@@ -221,17 +227,22 @@ def time_e2e(capi, prec, steps, device):
 ADJOINT = dict(dim=256, viscosity=0.0089, iterations=10000, checkpoint_every=100, plane_y=128)
 # the FP32-storage comparison, shorter
 ADJOINT_FP32 = dict(dim=256, viscosity=0.0089, iterations=400, checkpoint_every=20, plane_y=128)
+# the FP16 forward with a tau gradient too (full-state segments), shorter
+ADJOINT_TAU = dict(dim=256, viscosity=0.0089, iterations=2000, checkpoint_every=100, plane_y=128)
 
 
-def time_adjoint(capi, prec, device):
+def time_adjoint(capi, prec, device, with_tau=False):
     """Adjoint/forward time at 256^3: the plain forward iteration (CUDA
     events over 400 iterations) against the backward sweep of
     lbm_adjoint_backward (checkpoint segments recomputed + hand-written
     adjoint kernel), per iteration, with the checkpointed forward reported
-    too; peak device memory of the adjoint run."""
+    too; peak device memory of the adjoint run.  The specified control is the
+    lid field (gradients of the lid and of the initial populations, whose
+    sweep stores only velocities and lid densities per iteration);
+    with_tau adds the relaxation time (full-state segments)."""
     import torch
     from lbmcl_gb300.validate import smooth_lid
-    a = ADJOINT if prec in ("fp16", "bf16") else ADJOINT_FP32
+    a = ADJOINT_TAU if with_tau else (ADJOINT if prec in ("fp16", "bf16") else ADJOINT_FP32)
     dim, T, c = a["dim"], a["iterations"], a["checkpoint_every"]
     rng = np.random.default_rng(1234)
     target_lid = smooth_lid(dim, rng).reshape(-1)
@@ -258,13 +269,15 @@ def time_adjoint(capi, prec, device):
         L.adjoint_forward(T, c)
         t1 = time.perf_counter()
         free1 = torch.cuda.mem_get_info(device)[0]
-        L.adjoint_backward(1.0, want_f0=False)
+        L.adjoint_backward(1.0, want_f0=False, want_tau=with_tau)
         t2 = time.perf_counter()
         free2 = torch.cuda.mem_get_info(device)[0]
     ckpt_ms = (t1 - t0) * 1e3 / T
     bwd_ms = (t2 - t1) * 1e3 / T
     return {"dim": dim, "storage": prec, "adjoint": "fp32" if prec != "fp64" else "fp64", "iterations": T,
-            "checkpoint_every": c, "control": "per-column lid 0.05 + N(0, 0.005), tau, mid-plane u_x loss",
+            "checkpoint_every": c,
+            "control": "per-column lid 0.05 + N(0, 0.005)" + (" and tau" if with_tau else "") + ", mid-plane u_x loss",
+            "segments": "full states" if with_tau else "stored velocity / lid density per iteration",
             "forward_ms_per_iter": round(fwd_ms, 4),
             "checkpointed_forward_ms_per_iter": round(ckpt_ms, 4), "backward_ms_per_iter": round(bwd_ms, 4),
             "adjoint_over_forward": round(bwd_ms / fwd_ms, 3),
@@ -452,6 +465,7 @@ def main():
     adjoint = None
     if not args.no_adjoint:
         adjoint = {p: time_adjoint(capi, p, device) for p in ("fp16", "fp32")}
+        adjoint["fp16_with_tau"] = time_adjoint(capi, "fp16", device, with_tau=True)
     e2e_ms, h2d, d2h = time_e2e(capi, head, args.steps, device)
     e2e_mlups = wet * args.steps / (e2e_ms * 1e3) * ws
 

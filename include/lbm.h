@@ -106,6 +106,15 @@ typedef struct lbm_config {
                                   one captured CUDA graph (launch-bound small lattices);
                                   0 = default 16, 1 = launch every kernel directly; an
                                   even number, at most 256                                  */
+    int adjoint_full_states;   /* backward sweep without a tau gradient: 0 = recompute each
+                                  segment storing only the adjoint's linearisation point
+                                  per iteration (u of FLUID sites, rho of lid sites: 3
+                                  planes); 1 = store the full states, as with a tau
+                                  gradient                                                  */
+    int adjoint_fp64;          /* 1: the adjoint in FP64 arithmetic for FP32 / FP16 / BF16
+                                  storage too (one step per launch), e.g. to measure the
+                                  FP32 adjoint's rounding on the same trajectory; 0: FP64
+                                  only for FP64 storage                                     */
 } lbm_config;
 
 /* Iteration kernel variants (same results, different data movement). */
@@ -191,13 +200,17 @@ int lbm_adjoint_forward(lbm_t *h, int iterations, int checkpoint_every, double *
 
 /* Backward sweep of the last lbm_adjoint_forward, scaled by dloss (dL/dJ for
  * a caller's outer loss L): hand-written adjoint kernels, each checkpoint
- * segment recomputed with the forward kernel.  Any output may be NULL:
+ * segment recomputed with the forward kernel.  Without grad_tau the segments
+ * are recomputed storing only the velocity (FLUID) and density (lid sites) of
+ * each iteration, which is all the adjoint of the lid and of the initial
+ * populations needs (lbm_config.adjoint_full_states).  Any output may be NULL:
  *   grad_tau   dL/dtau
  *   grad_lid   dim*dim doubles, dL/dlid at [x + y*dim]
  *   grad_f0    dL/dR_0 in the LBM_DUMP_F layout and type (grad_f0_bytes =
  *              lbm_size(h, LBM_DUMP_F)); when R_0 is the state lbm_init made,
  *              its dependence on the lid is included in grad_lid.
- * Adjoint arithmetic: FP64 for an FP64 handle, FP32 otherwise.  Synchronous. */
+ * Adjoint arithmetic: FP64 for an FP64 handle or with adjoint_fp64, FP32
+ * otherwise.  Synchronous. */
 int lbm_adjoint_backward(lbm_t *h, double dloss, double *grad_tau, double *grad_lid, void *grad_f0,
                          size_t grad_f0_bytes);
 

@@ -45,12 +45,16 @@ class _CavityLoss(torch.autograd.Function):
     @staticmethod
     def backward(ctx, grad_out):
         L = ctx.lattice
-        g_tau, g_lid, g_f0 = L.adjoint_backward(float(grad_out), want_f0=ctx.has_f0)
+        # without a tau gradient the sweep stores only velocities / lid
+        # densities per iteration instead of full states
+        want_tau = bool(ctx.needs_input_grad[1])
+        g_tau, g_lid, g_f0 = L.adjoint_backward(float(grad_out), want_f0=ctx.has_f0, want_tau=want_tau)
         L.close()
         ctx.lattice = None
         lt, tt, ft = ctx.dtypes
         out_f0 = torch.from_numpy(np.ascontiguousarray(g_f0)).to(ft) if ctx.has_f0 else None
-        return (torch.from_numpy(g_lid).to(lt), torch.tensor(g_tau, dtype=tt), out_f0, None)
+        out_tau = torch.tensor(g_tau, dtype=tt) if want_tau else None
+        return (torch.from_numpy(g_lid).to(lt), out_tau, out_f0, None)
 
 
 def cavity_loss(lid: torch.Tensor, tau: torch.Tensor, f0, *, dim: int, iterations: int, plane_y: int,

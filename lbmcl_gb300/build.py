@@ -28,7 +28,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
                      "-I" + INCLUDE, "-I" + CSRC]
 CU_SOURCES = ["lbm_capi.cu", "lbm_kernels_f32.cu", "lbm_kernels_f64.cu", "lbm_kernels_f16.cu",
-              "lbm_kernels_bf16.cu", "lbm_noalloc.cu", "lbm_adjoint_host.cu"]
+              "lbm_kernels_bf16.cu", "lbm_noalloc.cu", "lbm_adjoint_host.cu", "lbm_adjoint_f64.cu"]
 HOST_SOURCES = ["host/main.cpp"]
 
 

@@ -50,6 +50,8 @@ class Config(C.Structure):
         ("adjoint_steps", C.c_int),
         ("adjoint_max_states", C.c_int),
         ("graph_iterations", C.c_int),
+        ("adjoint_full_states", C.c_int),
+        ("adjoint_fp64", C.c_int),
     ]
 
 
@@ -122,13 +124,16 @@ class Lattice:
     launch of the backward sweep (0 = default, 1, 2).  adjoint_max_states:
     cap on the backward sweep's recomputed state buffers (0 = as many as fit).
     graph_iterations: iterations per CUDA graph replay in step() (0 = 16,
-    1 = no graphs).
+    1 = no graphs).  adjoint_full_states: recompute full states in a backward
+    sweep without a tau gradient too (default: only the velocity / density
+    the adjoint needs).  adjoint_fp64: FP64 adjoint arithmetic over FP32 /
+    16-bit storage.
     """
 
     def __init__(self, dim, viscosity=0.0089, velocity=0.05, precision="fp32", stride=None, lid=None,
                  seed=0, noise_sigma=0.0, tau=0.0, block_threads=0, max_device_bytes=0, device=0,
                  profile_steps=False, kernel=0, stages=0, adjoint_steps=0, adjoint_max_states=0,
-                 graph_iterations=0):
+                 graph_iterations=0, adjoint_full_states=False, adjoint_fp64=False):
         L = lib()
         c = default_config()
         c.dim = int(dim)
@@ -152,6 +157,8 @@ class Lattice:
         c.adjoint_steps = int(adjoint_steps)
         c.adjoint_max_states = int(adjoint_max_states)
         c.graph_iterations = int(graph_iterations)
+        c.adjoint_full_states = 1 if adjoint_full_states else 0
+        c.adjoint_fp64 = 1 if adjoint_fp64 else 0
         self.cfg = c
         self.dim = int(dim)
         self.n = self.dim ** 3
@@ -260,16 +267,18 @@ class Lattice:
         check(lib().lbm_adjoint_forward(self.h, int(iterations), int(checkpoint_every), C.byref(loss)))
         return loss.value
 
-    def adjoint_backward(self, dloss: float = 1.0, want_f0: bool = True):
-        """Returns (dL/dtau, dL/dlid as [y, x], dL/dR_0 in the F layout or None)."""
+    def adjoint_backward(self, dloss: float = 1.0, want_f0: bool = True, want_tau: bool = True):
+        """Returns (dL/dtau or None, dL/dlid as [y, x], dL/dR_0 in the F layout
+        or None).  Without want_tau the sweep stores only the adjoint's
+        linearisation points (unless adjoint_full_states)."""
         gt = C.c_double()
         glid = np.zeros(self.dim * self.dim, np.float64)
         gf0 = np.empty(self.size(DUMP_F) // np.dtype(self.fdtype).itemsize, self.fdtype) if want_f0 else None
-        check(lib().lbm_adjoint_backward(self.h, float(dloss), C.byref(gt),
+        check(lib().lbm_adjoint_backward(self.h, float(dloss), C.byref(gt) if want_tau else None,
                                          glid.ctypes.data_as(C.POINTER(C.c_double)),
                                          gf0.ctypes.data_as(C.c_void_p) if gf0 is not None else None,
                                          gf0.nbytes if gf0 is not None else 0))
-        return gt.value, glid.reshape(self.dim, self.dim), gf0
+        return (gt.value if want_tau else None), glid.reshape(self.dim, self.dim), gf0
 
     def load_raw(self, raw: np.ndarray):
         raw = np.ascontiguousarray(raw)

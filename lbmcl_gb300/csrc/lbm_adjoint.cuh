@@ -84,16 +84,10 @@ template <class A> __device__ __forceinline__ A w_of(int i)
     return wclass_of(i) == 0 ? (A)1 / (A)3 : (wclass_of(i) == 1 ? (A)1 / (A)18 : (A)1 / (A)36);
 }
 
-// MOVING site.
+// MOVING site with density rho (of g after the -z replacements).
 template <class A>
-__device__ __forceinline__ void adjoint_moving(const A (&g)[Q], A (&b)[Q], A lid, A &dlid)
+__device__ __forceinline__ void adjoint_moving_rho(A (&b)[Q], A rho, A lid, A &dlid)
 {
-    A rho = 0;
-#pragma unroll
-    for (int i = 0; i < Q; ++i) {
-        const bool replaced = (i == 5 || i == 11 || i == 12 || i == 13 || i == 14);
-        rho += replaced ? g[opp_of(i)] : g[i];
-    }
     const A c15 = (A)1.5 * lid * lid;
     A s = 0, dl = 0;
 #pragma unroll
@@ -113,6 +107,19 @@ __device__ __forceinline__ void adjoint_moving(const A (&g)[Q], A (&b)[Q], A lid
     dlid += dl;
 }
 
+// MOVING site.
+template <class A>
+__device__ __forceinline__ void adjoint_moving(const A (&g)[Q], A (&b)[Q], A lid, A &dlid)
+{
+    A rho = 0;
+#pragma unroll
+    for (int i = 0; i < Q; ++i) {
+        const bool replaced = (i == 5 || i == 11 || i == 12 || i == 13 || i == 14);
+        rho += replaced ? g[opp_of(i)] : g[i];
+    }
+    adjoint_moving_rho<A>(b, rho, lid, dlid);
+}
+
 // FLUID adjoint written around opposite pairs (i, i') with e_i.u = +-a:
 //   p_(+-) = base +- 3a, base = 1 + 4.5 a^2 - 1.5 u^2
 //   B0 = sum_c w_c sum_pairs (s base + 3 a d),   s = b+ + b-, d = b+ - b-
@@ -120,19 +127,8 @@ __device__ __forceinline__ void adjoint_moving(const A (&g)[Q], A (&b)[Q], A lid
 //   a_(+-) = (1 - omega) b_(+-) + omega (B0 - G.u) +- omega G.e_i
 //   dJ/domega += rho B0 - sum_i b_i g_i
 template <class A>
-__device__ __forceinline__ void adjoint_fluid_pairs(const A (&g)[Q], A (&b)[Q], A omega, A &dw)
+__device__ __forceinline__ A adjoint_fluid_core(A (&b)[Q], A ux, A uy, A uz, A omega)
 {
-    A rho = 0, jx = 0, jy = 0, jz = 0, bg = 0;
-#pragma unroll
-    for (int i = 0; i < Q; ++i) {
-        rho += g[i];
-        if (ex_of(i)) jx += ex_of(i) > 0 ? g[i] : -g[i];
-        if (ey_of(i)) jy += ey_of(i) > 0 ? g[i] : -g[i];
-        if (ez_of(i)) jz += ez_of(i) > 0 ? g[i] : -g[i];
-        bg += b[i] * g[i];
-    }
-    const A inv = (A)1 / rho;
-    const A ux = jx * inv, uy = jy * inv, uz = jz * inv;
     const A c0 = (A)1 - (A)1.5 * (ux * ux + uy * uy + uz * uz);
     // per weight class accumulators: rest (0), axis (1), edge (2)
     A B[3] = {b[0] * c0, 0, 0}, SB[3] = {b[0], 0, 0};
@@ -173,12 +169,91 @@ __device__ __forceinline__ void adjoint_fluid_pairs(const A (&g)[Q], A (&b)[Q], 
         b[i] = keep * b[i] + (oc + t);
         b[j] = keep * b[j] + (oc - t);
     }
+    return B0;
+}
+
+// A FLUID site's pre-collision populations g (adjoint type) and its moments
+// as the forward's collision formed them from the stored values v: the
+// deviation-form sums for 16-bit storage (moments_dev), the reference's
+// summation order for FP32 / FP64 (moments_exact).
+template <class S, class A>
+__device__ __forceinline__ void forward_point(const S (&v)[Q], A (&g)[Q], A &rho, A &ux, A &uy, A &uz)
+{
+    if constexpr (is_dev16<S>()) {
+        float D[Q];
+#pragma unroll
+        for (int i = 0; i < Q; ++i) D[i] = Dev16<S>::to_f(v[i]);
+        float drho, r, x, y, z;
+        moments_dev(D, Dev16<S>::inv_scale, drho, r, x, y, z);
+        rho = (A)r;
+        ux = (A)x;
+        uy = (A)y;
+        uz = (A)z;
+#pragma unroll
+        for (int i = 0; i < Q; ++i) g[i] = (A)(wf_of(i) + D[i] * Dev16<S>::inv_scale);
+    } else {
+        using C = typename Compute<S>::type;
+        C f[Q];
+#pragma unroll
+        for (int i = 0; i < Q; ++i) f[i] = (C)v[i];
+        C r, x, y, z;
+        moments_exact(f, r, x, y, z);
+        rho = (A)r;
+        ux = (A)x;
+        uy = (A)y;
+        uz = (A)z;
+#pragma unroll
+        for (int i = 0; i < Q; ++i) g[i] = (A)f[i];
+    }
+}
+
+// FLUID site at the forward's point: the core, and dw += dJ/domega term
+// rho B0 - sum_i b_i g_i (b before the update).
+template <class A>
+__device__ __forceinline__ void adjoint_fluid_point(const A (&g)[Q], A (&b)[Q], A rho, A ux, A uy, A uz, A omega,
+                                                    A &dw)
+{
+    A bg = 0;
+#pragma unroll
+    for (int i = 0; i < Q; ++i) bg += b[i] * g[i];
+    const A B0 = adjoint_fluid_core<A>(b, ux, uy, uz, omega);
     dw += rho * B0 - bg;
 }
 
-// Any site kind (face rows): map-driven.  g gets the wall-sourced constants.
-template <class A, class C>
-__device__ __forceinline__ void adjoint_general(A (&g)[Q], A (&b)[Q], uint8_t b8, C lidv, A omega,
+// Any site kind from the forward's stored linearisation point (MODE_STEP_ADJ
+// planes m0, m1, m2: u of a FLUID site, rho of a MOVING site): the adjoint
+// without the tau term, which needs the full populations.
+template <class A>
+__device__ __forceinline__ void adjoint_site_macro(A (&b)[Q], uint8_t b8, A m0, A m1, A m2, A lidv, A omega,
+                                                   A &dlid)
+{
+    if (b8 == 0) {
+        adjoint_fluid_core<A>(b, m0, m1, m2, omega);
+        return;
+    }
+    if (b8 & M_WALL) {
+#pragma unroll
+        for (int i = 0; i < Q; ++i) b[i] = (A)0;
+        return;
+    }
+    if (b8 == M_FRONT) {
+        adjoint_moving_rho<A>(b, m0, lidv, dlid);
+        return;
+    }
+    if (!(b8 & M_CORNER)) {
+        A t[Q];
+#pragma unroll
+        for (int i = 0; i < Q; ++i) t[i] = b[opp_of(i)];
+#pragma unroll
+        for (int i = 0; i < Q; ++i) b[i] = t[i];
+    }
+}
+
+// Any site kind (face rows), map-driven, from the stored forward values v of
+// its pulled populations: FLUID at the forward's point; otherwise g gets the
+// wall-sourced constants.
+template <class S, class A, class C>
+__device__ __forceinline__ void adjoint_general(const S (&v)[Q], A (&b)[Q], uint8_t b8, C lidv, A omega,
                                                 const Weights<C> &W, A &dw, A &dlid)
 {
     if (b8 & M_WALL) {
@@ -187,13 +262,16 @@ __device__ __forceinline__ void adjoint_general(A (&g)[Q], A (&b)[Q], uint8_t b8
         return;
     }
     if (b8 == 0) {
-        adjoint_fluid_pairs<A>(g, b, omega, dw);
+        A g[Q], rho, ux, uy, uz;
+        forward_point<S, A>(v, g, rho, ux, uy, uz);
+        adjoint_fluid_point<A>(g, b, rho, ux, uy, uz, omega, dw);
         return;
     }
-#pragma unroll
-    for (int i = 0; i < Q; ++i)
-        if (wall_sourced(i, b8)) g[i] = (A)((b8 & M_FRONT) ? (C)init_eq_exact<C>(i, lidv, W) : W.w[wclass_of(i)]);
     if (b8 == M_FRONT) {
+        A g[Q];
+#pragma unroll
+        for (int i = 0; i < Q; ++i)
+            g[i] = wall_sourced(i, b8) ? (A)init_eq_exact<C>(i, lidv, W) : fwd_value<S, A>(v[i], i);
         adjoint_moving<A>(g, b, (A)lidv, dlid);
     } else if (!(b8 & M_CORNER)) {
         A t[Q];
@@ -227,12 +305,14 @@ __device__ __forceinline__ void adjoint_face_fix(const AdjArgs &a, size_t rowoff
 #ifndef LBM_ADJ_MINB
 #define LBM_ADJ_MINB 2
 #endif
-template <class S> constexpr int adj_min_blocks() { return sizeof(S) == 8 ? 1 : LBM_ADJ_MINB; }
 
-template <class S, int VB, int ROWS>
-__global__ void __launch_bounds__(256, adj_min_blocks<S>()) adjoint_kernel(AdjArgs a)
+// MACRO = false: a.fwd is the forward state Q_k (its pull gives the
+// pre-collision populations); MACRO = true: a.fwd holds the three planes the
+// MODE_STEP_ADJ iteration from Q_k stored (compute type), and no tau term is
+// formed.
+template <class S, class A, int VB, int ROWS, bool MACRO>
+__global__ void __launch_bounds__(256, sizeof(A) == 8 ? 1 : LBM_ADJ_MINB) adjoint_kernel(AdjArgs a)
 {
-    using A = typename AdjType<S>::type;
     using C = typename Compute<S>::type;
     constexpr int V = VB / (int)sizeof(A);
     const int dim = a.dim;
@@ -265,25 +345,39 @@ __global__ void __launch_bounds__(256, adj_min_blocks<S>()) adjoint_kernel(AdjAr
             else if (ex_of(i) == -1) gather_row<A, V, 1>(src, x0, dim, bs[i]);
             else gather_row<A, V, 0>(src, x0, dim, bs[i]);
         }
-        // forward pre-collision values R_k(s): the forward pull
-        const S *fwd = static_cast<const S *>(a.fwd);
-        S fsv[Q][V];
-        gather_all<S, V, 0>(fwd, a.n, rowoff, dim, x0, fsv);
         const A omega = (A)a.omega;
+        // forward values: the pulled populations R_k(s), or the stored
+        // linearisation point (three planes, same element type as A)
+        S fsv[MACRO ? 1 : Q][MACRO ? 1 : V];
+        C mv[MACRO ? 3 : 1][MACRO ? V : 1];
+        if constexpr (MACRO) {
+            const C *m = static_cast<const C *>(a.fwd);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) load_vec<C, V>(m + (size_t)c * a.n + site0, mv[c]);
+        } else {
+            const S *fwd = static_cast<const S *>(a.fwd);
+            gather_all<S, V, 0>(fwd, a.n, rowoff, dim, x0, fsv);
+        }
 
         if (ROWS == ROWS_INTERIOR) {
 #pragma unroll
             for (int k = 0; k < V; ++k) {
-                A g[Q], b[Q];
+                A b[Q];
 #pragma unroll
-                for (int i = 0; i < Q; ++i) {
-                    g[i] = fwd_value<S, A>(fsv[i][k], i);
-                    b[i] = bs[i][k];
+                for (int i = 0; i < Q; ++i) b[i] = bs[i][k];
+                if constexpr (MACRO) {
+                    adjoint_fluid_core<A>(b, (A)mv[0][k], (A)mv[1][k], (A)mv[2][k], omega);
+                } else {
+                    S v[Q];
+#pragma unroll
+                    for (int i = 0; i < Q; ++i) v[i] = fsv[i][k];
+                    A g[Q], rho, ux, uy, uz;
+                    forward_point<S, A>(v, g, rho, ux, uy, uz);
+                    A d = 0;
+                    adjoint_fluid_point<A>(g, b, rho, ux, uy, uz, omega, d);
+                    // x in [2, dim-3] is FLUID; the row ends are patched below
+                    if ((unsigned)(x0 + k - 2) <= (unsigned)(dim - 5)) dw += d;
                 }
-                A d = 0;
-                adjoint_fluid_pairs<A>(g, b, omega, d);
-                // x in [2, dim-3] is FLUID; the row ends are patched below
-                if ((unsigned)(x0 + k - 2) <= (unsigned)(dim - 5)) dw += d;
 #pragma unroll
                 for (int i = 0; i < Q; ++i) bs[i][k] = b[i];
             }
@@ -305,15 +399,19 @@ __global__ void __launch_bounds__(256, adj_min_blocks<S>()) adjoint_kernel(AdjAr
 #pragma unroll
             for (int k = 0; k < V; ++k) {
                 const uint8_t b8 = (uint8_t)(mw >> (8 * k));
-                A g[Q], b[Q];
+                A b[Q];
 #pragma unroll
-                for (int i = 0; i < Q; ++i) {
-                    g[i] = fwd_value<S, A>(fsv[i][k], i);
-                    b[i] = bs[i][k];
-                }
+                for (int i = 0; i < Q; ++i) b[i] = bs[i][k];
                 const C lidv = (b8 & M_FRONT) ? lid[(size_t)y * dim + x0 + k] : (C)0;
                 A dl = 0;
-                adjoint_general<A, C>(g, b, b8, lidv, omega, W, dw, dl);
+                if constexpr (MACRO) {
+                    adjoint_site_macro<A>(b, b8, (A)mv[0][k], (A)mv[1][k], (A)mv[2][k], (A)lidv, omega, dl);
+                } else {
+                    S v[Q];
+#pragma unroll
+                    for (int i = 0; i < Q; ++i) v[i] = fsv[i][k];
+                    adjoint_general<S, A, C>(v, b, b8, lidv, omega, W, dw, dl);
+                }
                 if (b8 == M_FRONT) a.grad_lid[(size_t)y * dim + x0 + k] += (double)dl;
 #pragma unroll
                 for (int i = 0; i < Q; ++i) bs[i][k] = b[i];
@@ -323,7 +421,7 @@ __global__ void __launch_bounds__(256, adj_min_blocks<S>()) adjoint_kernel(AdjAr
 #pragma unroll
         for (int i = 0; i < Q; ++i) store_vec<A, V>(aout + (size_t)i * a.n + site0, bs[i]);
     }
-    block_reduce_add((double)dw, a.tau_acc + a.tau_base);
+    if constexpr (!MACRO) block_reduce_add((double)dw, a.tau_acc + a.tau_base);
 }
 
 // ---------------------------------------------------------------------------
@@ -399,27 +497,41 @@ struct Adj2Args {
 #ifndef LBM_ADJ2_MINB
 #define LBM_ADJ2_MINB 3
 #endif
+// resident blocks per SM of the MACRO variant (no pulled populations in
+// registers)
+#ifndef LBM_ADJ2M_MINB
+#define LBM_ADJ2M_MINB 3
+#endif
 
-// a_k(s) of one site of step A or B: b = the reverse-streamed adjoint,
-// fwd = Q of the step; d, l = its tau and lid terms.
+// a_k(s) of one site of step A or B: b = the reverse-streamed adjoint, v =
+// the stored forward values of its pulled populations; d, l = its tau and
+// lid terms.
 template <class S>
-__device__ __forceinline__ void adjoint_site(float (&g)[Q], uint8_t b8, float lidv, float omega,
+__device__ __forceinline__ void adjoint_site(const S (&v)[Q], uint8_t b8, float lidv, float omega,
                                              const Weights<float> &W, float (&b)[Q], float &d, float &l)
 {
-    if (b8 == 0) adjoint_fluid_pairs<float>(g, b, omega, d);
-    else adjoint_general<float, float>(g, b, b8, lidv, omega, W, d, l);
+    if (b8 == 0) {
+        float g[Q], rho, ux, uy, uz;
+        forward_point<S, float>(v, g, rho, ux, uy, uz);
+        adjoint_fluid_point<float>(g, b, rho, ux, uy, uz, omega, d);
+    } else {
+        adjoint_general<S, float, float>(v, b, b8, lidv, omega, W, d, l);
+    }
 }
-// the forward pull R(s) of a site from its step's Q
+// the stored values of a site's forward pull from its step's Q
 template <class S>
 __device__ __forceinline__ void adjoint_pull(const S *__restrict__ fwd, const unsigned (&off)[Q], unsigned site,
-                                             float (&g)[Q])
+                                             S (&v)[Q])
 {
 #pragma unroll
-    for (int i = 0; i < Q; ++i) g[i] = fwd_value<S, float>(load_one(fwd + (site + off[i])), i);
+    for (int i = 0; i < Q; ++i) v[i] = load_one(fwd + (site + off[i]));
 }
 
-template <class S>
-__global__ void __launch_bounds__(ADJ2_EX * ADJ2_EY, LBM_ADJ2_MINB) adjoint2_kernel(Adj2Args a)
+// MACRO = true: fwd_a / fwd_b hold the three MODE_STEP_ADJ planes (float) of
+// Q_k / Q_{k-1} instead of the states, and no tau term is formed.
+template <class S, bool MACRO>
+__global__ void __launch_bounds__(ADJ2_EX * ADJ2_EY, MACRO ? LBM_ADJ2M_MINB : LBM_ADJ2_MINB)
+    adjoint2_kernel(Adj2Args a)
 {
     extern __shared__ float adj2_smem[];  // [ADJ2_SLOTS][ADJ2_EY][ADJ2_EX]
     constexpr int PL = ADJ2_EX * ADJ2_EY;
@@ -465,11 +577,17 @@ __global__ void __launch_bounds__(ADJ2_EX * ADJ2_EY, LBM_ADJ2_MINB) adjoint2_ker
             } else {
 #pragma unroll
                 for (int i = 0; i < Q; ++i) b[i] = __ldg(a.ain + (site + a.off_up[i]));
-                float g[Q];
-                adjoint_pull<S>(fwd_a, a.off_down, site, g);
                 float d = 0.f, l = 0.f;
                 const float lidv = (b8 & M_FRONT) ? lid[col] : 0.f;
-                adjoint_site<S>(g, b8, lidv, omega, W, b, d, l);
+                if constexpr (MACRO) {
+                    const float *m = static_cast<const float *>(a.fwd_a);
+                    adjoint_site_macro<float>(b, b8, __ldg(m + site), __ldg(m + (site + a.off_own[1])),
+                                              __ldg(m + (site + a.off_own[2])), lidv, omega, l);
+                } else {
+                    S v[Q];
+                    adjoint_pull<S>(fwd_a, a.off_down, site, v);
+                    adjoint_site<S>(v, b8, lidv, omega, W, b, d, l);
+                }
                 if (owned && p >= zi0 && p < zi1) {
                     dw += d;
                     dl += l;
@@ -492,11 +610,19 @@ __global__ void __launch_bounds__(ADJ2_EX * ADJ2_EY, LBM_ADJ2_MINB) adjoint2_ker
         const int q = p - 1;
         const bool do_b = owned && q >= zi0;
         const unsigned site_b = (unsigned)q * plane + col;
-        float gb[Q];
+        float mb[3];
+        S vb[MACRO ? 1 : Q];
         uint8_t b8b = 0;
         if (do_b) {  // owned sites are never walls
             b8b = (own_fluid && q >= 2 && q <= dim - 3) ? (uint8_t)0 : __ldg(a.map + site_b);
-            adjoint_pull<S>(fwd_b, a.off_down, site_b, gb);
+            if constexpr (MACRO) {
+                const float *m = static_cast<const float *>(a.fwd_b);
+                mb[0] = __ldg(m + site_b);
+                mb[1] = __ldg(m + (site_b + a.off_own[1]));
+                mb[2] = __ldg(m + (site_b + a.off_own[2]));
+            } else {
+                adjoint_pull<S>(fwd_b, a.off_down, site_b, vb);
+            }
         }
         __syncthreads();
         if (do_b) {
@@ -516,7 +642,8 @@ __global__ void __launch_bounds__(ADJ2_EX * ADJ2_EY, LBM_ADJ2_MINB) adjoint2_ker
             b[6] = r6;
             float d = 0.f, l = 0.f;
             const float lidv = (b8 & M_FRONT) ? lid[col] : 0.f;
-            adjoint_site<S>(gb, b8, lidv, omega, W, b, d, l);
+            if constexpr (MACRO) adjoint_site_macro<float>(b, b8, mb[0], mb[1], mb[2], lidv, omega, l);
+            else adjoint_site<S>(vb, b8, lidv, omega, W, b, d, l);
             dw += d;
             dl += l;
 #pragma unroll
@@ -528,7 +655,7 @@ __global__ void __launch_bounds__(ADJ2_EX * ADJ2_EY, LBM_ADJ2_MINB) adjoint2_ker
     }
     // one MOVING site per column, in one chunk: a single writer per column
     if (owned && zi0 <= dim - 2 && dim - 2 < zi1) a.grad_lid[col] += (double)dl;
-    block_reduce_add((double)dw, a.tau_acc);
+    if constexpr (!MACRO) block_reduce_add((double)dw, a.tau_acc);
 }
 
 // Seed of the backward sweep: a_T = dJ/dR_T for the mid-plane loss
@@ -536,10 +663,9 @@ __global__ void __launch_bounds__(ADJ2_EX * ADJ2_EY, LBM_ADJ2_MINB) adjoint2_ker
 // dJ/dR_T(s, i) = (2/M) (u_x - target) (e_ix - u_x) / rho; zero elsewhere.
 // a.dloss carries the factor dJ_total/dJ * 2 / M.  Also writes the loss
 // partials (sum of squared differences) when loss_part != NULL.
-template <class S>
+template <class S, class A>
 __global__ void __launch_bounds__(256) loss_seed_kernel(AdjArgs a)
 {
-    using A = typename AdjType<S>::type;
     const int dim = a.dim;
     const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     double sq = 0.0;
@@ -579,10 +705,9 @@ __global__ void __launch_bounds__(256) loss_seed_kernel(AdjArgs a)
 // sites (x, y in [1, dim-2], z = dim-2) start at the equilibrium at rho = 1
 // and u = (lid, 0, 0) (kernels.cl:292-308); dR_0(s,i)/dlid =
 // w_i (3 e_ix + (9 e_ix^2 - 3) lid).
-template <class S>
+template <class S, class A>
 __global__ void lid_init_grad_kernel(AdjArgs a)
 {
-    using A = typename AdjType<S>::type;
     using C = typename Compute<S>::type;
     const int dim = a.dim;
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -601,9 +726,10 @@ __global__ void lid_init_grad_kernel(AdjArgs a)
     a.grad_lid[k] += s;
 }
 
-// Adjoint buffer (post-stream layout) -> CSoA order of the F dumps.
-template <class A>
-__global__ void export_adjoint_kernel(const A *__restrict__ adj, A *__restrict__ out, size_t o0, size_t count, int sd,
+// Adjoint buffer (post-stream layout) -> CSoA order of the F dumps, in the
+// dump element type T.
+template <class A, class T>
+__global__ void export_adjoint_kernel(const A *__restrict__ adj, T *__restrict__ out, size_t o0, size_t count, int sd,
                                       size_t n)
 {
     const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -611,7 +737,14 @@ __global__ void export_adjoint_kernel(const A *__restrict__ adj, A *__restrict__
     size_t id;
     int q;
     decode_csoa(o0 + k, sd, n, id, q);
-    out[k] = adj[(size_t)q * n + id];
+    out[k] = (T)adj[(size_t)q * n + id];
 }
+
+// Launchers of the FP64 adjoint over FP32 / 16-bit storage (their own
+// translation unit, lbm_adjoint_f64.cu): prec is the storage lbm_precision.
+cudaError_t launch_adjoint_step_a64(int prec, const AdjArgs &a, unsigned gi, unsigned gf, unsigned block,
+                                    cudaStream_t s, bool macro);
+cudaError_t launch_loss_seed_a64(int prec, const AdjArgs &a, unsigned grid, unsigned block, cudaStream_t s);
+cudaError_t launch_lid_init_grad_a64(int prec, const AdjArgs &a, cudaStream_t s);
 
 }  // namespace lbm

@@ -52,7 +52,9 @@ int fail(int code, const char *fmt, ...)
         }                                                                                            \
     } while (0)
 
-size_t adj_bytes(int prec) { return prec == LBM_FP64 ? 8 : 4; }
+// FP64 adjoint arithmetic: FP64 storage, or asked for (lbm_config.adjoint_fp64)
+bool adj64(const lbm_t *h) { return h->prec == LBM_FP64 || h->cfg.adjoint_fp64 != 0; }
+size_t adj_bytes(const lbm_t *h) { return adj64(h) ? 8 : 4; }
 // adjoint kernels: 2 sites per thread (8-byte FP32 / 16-byte FP64 vectors)
 constexpr int kAdjV = 2;
 
@@ -82,32 +84,33 @@ lbm::AdjArgs adj_args(const lbm_t *h)
     return a;
 }
 
-template <class S>
+template <class S, bool MACRO>
 cudaError_t run_adjoint_step(const lbm::AdjArgs &a0, unsigned gi, unsigned gf, cudaStream_t s)
 {
-    constexpr int VB = kAdjV * (int)sizeof(typename lbm::AdjType<S>::type);
+    using A = typename lbm::AdjType<S>::type;
+    constexpr int VB = kAdjV * (int)sizeof(A);
     lbm::AdjArgs a = a0;
     if (gi > 0) {
         a.tau_base = 0;
-        lbm::adjoint_kernel<S, VB, lbm::ROWS_INTERIOR><<<gi, kAdjBlock, 0, s>>>(a);
+        lbm::adjoint_kernel<S, A, VB, lbm::ROWS_INTERIOR, MACRO><<<gi, kAdjBlock, 0, s>>>(a);
         const cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
     a.tau_base = gi;
-    lbm::adjoint_kernel<S, VB, lbm::ROWS_FACES><<<gf, kAdjBlock, 0, s>>>(a);
+    lbm::adjoint_kernel<S, A, VB, lbm::ROWS_FACES, MACRO><<<gf, kAdjBlock, 0, s>>>(a);
     return cudaGetLastError();
 }
 template <class S>
 cudaError_t run_loss_seed(const lbm::AdjArgs &a, unsigned grid, cudaStream_t s)
 {
-    lbm::loss_seed_kernel<S><<<grid, kLossBlock, 0, s>>>(a);
+    lbm::loss_seed_kernel<S, typename lbm::AdjType<S>::type><<<grid, kLossBlock, 0, s>>>(a);
     return cudaGetLastError();
 }
 template <class S>
 cudaError_t run_lid_init_grad(const lbm::AdjArgs &a, cudaStream_t s)
 {
     const int nc = a.dim * a.dim;
-    lbm::lid_init_grad_kernel<S><<<(nc + 255) / 256, 256, 0, s>>>(a);
+    lbm::lid_init_grad_kernel<S, typename lbm::AdjType<S>::type><<<(nc + 255) / 256, 256, 0, s>>>(a);
     return cudaGetLastError();
 }
 
@@ -128,36 +131,46 @@ unsigned adj2_grid(const lbm_t *h, int &ntx, int &nty)
 // more: a small lattice (64^3: 66 blocks) runs faster one step at a time.
 bool two_step(const lbm_t *h)
 {
-    if (h->prec == LBM_FP64 || h->cfg.adjoint_steps == 1 || h->dim > lbm::ADJ2_MAX_DIM) return false;
+    if (adj64(h) || h->cfg.adjoint_steps == 1 || h->dim > lbm::ADJ2_MAX_DIM) return false;
     if (h->cfg.adjoint_steps == 2) return true;
     int ntx, nty;
     return adj2_grid(h, ntx, nty) >= 2u * (unsigned)std::max(h->num_sms, 1);
 }
 
-template <class S>
+template <class S, bool MACRO>
 cudaError_t run_adjoint2(const lbm::Adj2Args &a, unsigned grid, cudaStream_t s)
 {
-    lbm::adjoint2_kernel<S><<<grid, lbm::ADJ2_EX * lbm::ADJ2_EY, lbm::ADJ2_SMEM, s>>>(a);
+    lbm::adjoint2_kernel<S, MACRO><<<grid, lbm::ADJ2_EX * lbm::ADJ2_EY, lbm::ADJ2_SMEM, s>>>(a);
     return cudaGetLastError();
 }
 
-// The two-step kernel's shared-memory size, set at the start of every
+template <class S>
+cudaError_t set_adjoint2_smem()
+{
+    const int bytes = (int)lbm::ADJ2_SMEM;
+    const cudaFuncAttribute at = cudaFuncAttributeMaxDynamicSharedMemorySize;
+    cudaError_t e = cudaFuncSetAttribute(lbm::adjoint2_kernel<S, false>, at, bytes);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(lbm::adjoint2_kernel<S, true>, at, bytes);
+    return e;
+}
+
+// The two-step kernels' shared-memory size, set at the start of every
 // backward sweep (outside any graph capture): the attribute belongs to the
 // current device's context, and handles may live on different devices.
 cudaError_t prepare_adjoint2(const lbm_t *h)
 {
-    const int bytes = (int)lbm::ADJ2_SMEM;
-    const cudaFuncAttribute at = cudaFuncAttributeMaxDynamicSharedMemorySize;
     switch (h->prec) {
-    case LBM_FP32: return cudaFuncSetAttribute(lbm::adjoint2_kernel<float>, at, bytes);
-    case LBM_FP16: return cudaFuncSetAttribute(lbm::adjoint2_kernel<__half>, at, bytes);
-    case LBM_BF16: return cudaFuncSetAttribute(lbm::adjoint2_kernel<__nv_bfloat16>, at, bytes);
+    case LBM_FP32: return set_adjoint2_smem<float>();
+    case LBM_FP16: return set_adjoint2_smem<__half>();
+    case LBM_BF16: return set_adjoint2_smem<__nv_bfloat16>();
     default: return cudaSuccess;
     }
 }
 
-// a_{k+1} -> a_{k-1} with Q_k (fwd_a) and Q_{k-1} (fwd_b)
-cudaError_t adjoint_two_steps(const lbm_t *h, const void *fwd_a, const void *fwd_b, const void *ain, void *aout)
+// a_{k+1} -> a_{k-1} with Q_k (fwd_a) and Q_{k-1} (fwd_b), or with their
+// stored linearisation points (macro)
+cudaError_t adjoint_two_steps(const lbm_t *h, const void *fwd_a, const void *fwd_b, const void *ain, void *aout,
+                              bool macro)
 {
     lbm::Adj2Args a = {};
     a.fwd_a = fwd_a;
@@ -181,26 +194,39 @@ cudaError_t adjoint_two_steps(const lbm_t *h, const void *fwd_a, const void *fwd
     a.omega = (float)h->inv_tau;
     const unsigned grid = adj2_grid(h, a.ntx, a.nty);
     switch (h->prec) {
-    case LBM_FP32: return run_adjoint2<float>(a, grid, h->stream);
-    case LBM_FP16: return run_adjoint2<__half>(a, grid, h->stream);
-    default: return run_adjoint2<__nv_bfloat16>(a, grid, h->stream);
+    case LBM_FP32: return macro ? run_adjoint2<float, true>(a, grid, h->stream) : run_adjoint2<float, false>(a, grid, h->stream);
+    case LBM_FP16:
+        return macro ? run_adjoint2<__half, true>(a, grid, h->stream) : run_adjoint2<__half, false>(a, grid, h->stream);
+    default:
+        return macro ? run_adjoint2<__nv_bfloat16, true>(a, grid, h->stream)
+                     : run_adjoint2<__nv_bfloat16, false>(a, grid, h->stream);
     }
 }
 
-cudaError_t adjoint_step(const lbm_t *h, const lbm::AdjArgs &a)
+template <class S>
+cudaError_t run_adjoint_step_any(const lbm::AdjArgs &a, unsigned gi, unsigned gf, cudaStream_t s, bool macro)
+{
+    return macro ? run_adjoint_step<S, true>(a, gi, gf, s) : run_adjoint_step<S, false>(a, gi, gf, s);
+}
+
+cudaError_t adjoint_step(const lbm_t *h, const lbm::AdjArgs &a, bool macro)
 {
     unsigned gi, gf;
     adj_grids(h, gi, gf);
+    if (adj64(h) && h->prec != LBM_FP64)
+        return lbm::launch_adjoint_step_a64(h->prec, a, gi, gf, kAdjBlock, h->stream, macro);
     switch (h->prec) {
-    case LBM_FP32: return run_adjoint_step<float>(a, gi, gf, h->stream);
-    case LBM_FP64: return run_adjoint_step<double>(a, gi, gf, h->stream);
-    case LBM_FP16: return run_adjoint_step<__half>(a, gi, gf, h->stream);
-    default: return run_adjoint_step<__nv_bfloat16>(a, gi, gf, h->stream);
+    case LBM_FP32: return run_adjoint_step_any<float>(a, gi, gf, h->stream, macro);
+    case LBM_FP64: return run_adjoint_step_any<double>(a, gi, gf, h->stream, macro);
+    case LBM_FP16: return run_adjoint_step_any<__half>(a, gi, gf, h->stream, macro);
+    default: return run_adjoint_step_any<__nv_bfloat16>(a, gi, gf, h->stream, macro);
     }
 }
 
 cudaError_t loss_seed(const lbm_t *h, const lbm::AdjArgs &a)
 {
+    if (adj64(h) && h->prec != LBM_FP64)
+        return lbm::launch_loss_seed_a64(h->prec, a, h->adj.loss_grid, kLossBlock, h->stream);
     switch (h->prec) {
     case LBM_FP32: return run_loss_seed<float>(a, h->adj.loss_grid, h->stream);
     case LBM_FP64: return run_loss_seed<double>(a, h->adj.loss_grid, h->stream);
@@ -211,6 +237,7 @@ cudaError_t loss_seed(const lbm_t *h, const lbm::AdjArgs &a)
 
 cudaError_t lid_init_grad(const lbm_t *h, const lbm::AdjArgs &a)
 {
+    if (adj64(h) && h->prec != LBM_FP64) return lbm::launch_lid_init_grad_a64(h->prec, a, h->stream);
     switch (h->prec) {
     case LBM_FP32: return run_lid_init_grad<float>(a, h->stream);
     case LBM_FP64: return run_lid_init_grad<double>(a, h->stream);
@@ -253,15 +280,16 @@ void free_tracked(lbm_t *h, void *p, size_t bytes)
     h->adj.bytes -= bytes;
 }
 
-// The adjoint steps k = start + len - 1 .. start with Q_k given by state(k).
+// The adjoint steps k = start + len - 1 .. start with Q_k (or, macro, its
+// stored linearisation point) given by state(k).
 template <class State>
-int adjoint_steps_down(lbm_t *h, int start, int len, State state, int &cur)
+int adjoint_steps_down(lbm_t *h, int start, int len, State state, int &cur, bool macro = false)
 {
     lbm_adjoint_state &s = h->adj;
     int k = start + len - 1;
     if (two_step(h)) {
         for (; k - 1 >= start; k -= 2) {
-            ADJ_CUDA(adjoint_two_steps(h, state(k), state(k - 1), s.adj[cur], s.adj[cur ^ 1]));
+            ADJ_CUDA(adjoint_two_steps(h, state(k), state(k - 1), s.adj[cur], s.adj[cur ^ 1], macro));
             cur ^= 1;
         }
     }
@@ -270,10 +298,26 @@ int adjoint_steps_down(lbm_t *h, int start, int len, State state, int &cur)
         b.fwd = state(k);
         b.ain = s.adj[cur];
         b.aout = s.adj[cur ^ 1];
-        ADJ_CUDA(adjoint_step(h, b));
+        ADJ_CUDA(adjoint_step(h, b, macro));
         cur ^= 1;
     }
     return LBM_OK;
+}
+
+// Backward sweep over the iterations [start, start + len) from Q_start in q0,
+// storing linearisation points only: len iterations recomputed from q0 (the
+// states ping-pong through s.mtmp) write the point of each iteration k into
+// s.mseg[k - start], then the adjoint steps read them.  Needs len <= mseg.
+int sweep_macro(lbm_t *h, const void *q0, int start, int len, int &cur)
+{
+    lbm_adjoint_state &s = h->adj;
+    const void *in = q0;
+    for (int m = 0; m < len; ++m) {
+        void *out = s.mtmp[m & 1];
+        ADJ_CUDA(lbm::launch_iteration_adj(h, in, out, s.mseg[m]));
+        in = out;
+    }
+    return adjoint_steps_down(h, start, len, [&](int k) -> const void * { return s.mseg[k - start]; }, cur, true);
 }
 
 // Backward sweep over the iterations [start, start + len), Q_start in q0,
@@ -356,19 +400,24 @@ int sweep(lbm_t *h, const void *q0, int start, int len, const std::vector<void *
 // from the staged first state s.q0, then its c adjoint steps) as a captured
 // CUDA graph, replayed for every full segment: the launches of a launch-bound
 // small lattice cost one graph launch.  One graph per adjoint-buffer parity.
-int replay_segment(lbm_t *h, int c, int &cur)
+int replay_segment(lbm_t *h, int c, int &cur, bool macro)
 {
     lbm_adjoint_state &s = h->adj;
     cudaGraphExec_t &exec = s.seg_exec[cur];
     if (!exec) {
         ADJ_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
         int c2 = cur, rc = LBM_OK;
-        for (int m = 1; m < c && rc == LBM_OK; ++m) {
-            const cudaError_t e = lbm::launch_iteration(h, m == 1 ? s.q0 : s.seg[m - 2], s.seg[m - 1]);
-            if (e != cudaSuccess) rc = fail(LBM_ECUDA, "segment capture: %s", cudaGetErrorString(e));
+        if (macro) {
+            rc = sweep_macro(h, s.q0, 0, c, c2);
+        } else {
+            for (int m = 1; m < c && rc == LBM_OK; ++m) {
+                const cudaError_t e = lbm::launch_iteration(h, m == 1 ? s.q0 : s.seg[m - 2], s.seg[m - 1]);
+                if (e != cudaSuccess) rc = fail(LBM_ECUDA, "segment capture: %s", cudaGetErrorString(e));
+            }
+            if (rc == LBM_OK)
+                rc = adjoint_steps_down(h, 0, c, [&](int k) -> const void * { return k == 0 ? s.q0 : s.seg[k - 1]; },
+                                        c2);
         }
-        if (rc == LBM_OK)
-            rc = adjoint_steps_down(h, 0, c, [&](int k) -> const void * { return k == 0 ? s.q0 : s.seg[k - 1]; }, c2);
         cudaGraph_t g = nullptr;
         const cudaError_t ec = cudaStreamEndCapture(h->stream, &g);
         if (rc == LBM_OK && ec != cudaSuccess) rc = fail(LBM_ECUDA, "segment capture: %s", cudaGetErrorString(ec));
@@ -396,8 +445,14 @@ void release_adjoint(lbm_t *h)
     lbm_adjoint_state &s = h->adj;
     for (void *p : s.ckpt) cudaFree(p);
     for (void *p : s.seg) cudaFree(p);
+    for (void *p : s.mseg) cudaFree(p);
     s.ckpt.clear();
     s.seg.clear();
+    s.mseg.clear();
+    for (void *&p : s.mtmp) {
+        if (p) cudaFree(p);
+        p = nullptr;
+    }
     for (void *&p : s.adj) {
         if (p) cudaFree(p);
         p = nullptr;
@@ -425,7 +480,7 @@ int lbm_adjoint_set_loss(lbm_t *h, int plane_y, const double *target_ux)
         return fail(LBM_EINVAL, "lbm_adjoint_set_loss: plane_y %d must hold FLUID sites ([2, %d])", plane_y,
                     h->dim - 3);
     const size_t nc = (size_t)h->dim * h->dim;
-    const size_t ab = adj_bytes(h->prec);
+    const size_t ab = adj_bytes(h);
     if (!h->adj.target) {
         int rc = alloc_tracked(h, &h->adj.target, nc * ab);
         if (rc != LBM_OK) return rc;
@@ -527,10 +582,13 @@ int lbm_adjoint_backward(lbm_t *h, double dloss, double *grad_tau, double *grad_
     lbm_adjoint_state &s = h->adj;
     if (!s.ready || s.it_end != h->it)
         return fail(LBM_ESTATE, "lbm_adjoint_backward: no adjoint forward recorded for the current state");
-    const size_t ab = adj_bytes(h->prec);
+    const size_t ab = adj_bytes(h);
     const size_t abytes = (size_t)lbm::Q * h->n * ab;
-    if (grad_f0 && grad_f0_bytes != abytes)
-        return fail(LBM_EINVAL, "lbm_adjoint_backward: grad_f0 is %zu bytes, needs %zu", grad_f0_bytes, abytes);
+    // grad_f0 comes in the F dump's element type (double for FP64 storage)
+    const size_t db = h->prec == LBM_FP64 ? 8 : 4;
+    const size_t dbytes = (size_t)lbm::Q * h->n * db;
+    if (grad_f0 && grad_f0_bytes != dbytes)
+        return fail(LBM_EINVAL, "lbm_adjoint_backward: grad_f0 is %zu bytes, needs %zu", grad_f0_bytes, dbytes);
     const size_t nc = (size_t)h->dim * h->dim;
     unsigned gi, gf;
     adj_grids(h, gi, gf);
@@ -569,21 +627,69 @@ int lbm_adjoint_backward(lbm_t *h, double dloss, double *grad_tau, double *grad_
     a.dloss = m > 0 ? dloss * 2.0 / m : 0.0;
     ADJ_CUDA(loss_seed(h, a));
 
-    // segment states: c - 1 when they fit (one-level sqrt checkpointing),
-    // else as many as fit, and the sweep recurses.  Allocated on the first
-    // backward sweep only, so a loss-only forward holds just its checkpoints.
     const int T = s.iterations, c = s.every;
     const size_t fbytes = (size_t)lbm::Q * h->n * lbm::storage_bytes(h->prec);
-    if ((int)s.seg.size() < c - 1) {
-        size_t freeb = 0, totalb = 0;
-        ADJ_CUDA(cudaMemGetInfo(&freeb, &totalb));
-        const size_t margin = ((size_t)1 << 30) + totalb / 50;  // for the runtime and other users
-        size_t fit = freeb > margin ? (freeb - margin) / fbytes : 0;
-        const size_t cap = h->cfg.max_device_bytes;  // the handle's budget, if any
+    const size_t mbytes = 3 * h->n * lbm::macro_bytes(h->prec);
+    size_t freeb = 0, totalb = 0;
+    // device bytes this sweep may still take: free memory less a margin for
+    // the runtime and other users, within the handle's budget
+    auto room = [&]() -> size_t {
+        if (cudaMemGetInfo(&freeb, &totalb) != cudaSuccess) return 0;
+        const size_t margin = ((size_t)1 << 30) + totalb / 50;
+        size_t r = freeb > margin ? freeb - margin : 0;
+        const size_t cap = h->cfg.max_device_bytes;
         if (cap > 0) {
-            const size_t used = h->base_bytes + h->adj.bytes;
-            fit = std::min(fit, cap > used ? (cap - used) / fbytes : (size_t)0);
+            const size_t used = h->base_bytes + s.bytes;
+            r = std::min(r, cap > used ? cap - used : (size_t)0);
         }
+        return r;
+    };
+
+    // Without a tau gradient the adjoint needs only the velocity of the FLUID
+    // sites and the density of the lid sites of each iteration: the segments
+    // are recomputed storing those three planes (c of them, plus two state
+    // scratch buffers) instead of c - 1 full states.
+    bool macro = grad_tau == nullptr && !h->cfg.adjoint_full_states;
+    if (macro) {
+        // the full-state buffers of an earlier sweep make room first (and
+        // the graphs that captured them go)
+        if (!s.seg.empty()) drop_segment_graphs(s);
+        for (void *p : s.seg) free_tracked(h, p, fbytes);
+        s.seg.clear();
+        const size_t need = (s.mseg.size() < (size_t)c ? (size_t)c - s.mseg.size() : 0) * mbytes +
+                            (s.mtmp[0] ? 0 : 2 * fbytes);
+        if (need > room()) {
+            macro = false;  // does not fit: the full-state sweep (recursive when short)
+        } else {
+            for (int k = 0; k < 2; ++k)
+                if (!s.mtmp[k]) {
+                    const int rc = alloc_tracked(h, &s.mtmp[k], fbytes);
+                    if (rc != LBM_OK) return rc;
+                }
+            while ((int)s.mseg.size() < c) {
+                void *p = nullptr;
+                const int rc = alloc_tracked(h, &p, mbytes);
+                if (rc != LBM_OK) return rc;
+                s.mseg.push_back(p);
+            }
+        }
+    }
+    if (!macro) {
+        if (!s.mseg.empty() || s.mtmp[0] || s.mtmp[1]) drop_segment_graphs(s);
+        for (void *p : s.mseg) free_tracked(h, p, mbytes);
+        s.mseg.clear();
+        for (void *&p : s.mtmp) {
+            free_tracked(h, p, fbytes);
+            p = nullptr;
+        }
+    }
+
+    // full-state sweep: c - 1 segment states when they fit (one-level sqrt
+    // checkpointing), else as many as fit, and the sweep recurses.  Allocated
+    // on the first backward sweep only, so a loss-only forward holds just its
+    // checkpoints.
+    if (!macro && (int)s.seg.size() < c - 1) {
+        size_t fit = room() / fbytes;
         size_t want_total = (size_t)(c - 1);
         if (h->cfg.adjoint_max_states > 0) want_total = std::min(want_total, (size_t)h->cfg.adjoint_max_states);
         if (want_total > s.seg.size() + fit) {
@@ -607,28 +713,25 @@ int lbm_adjoint_backward(lbm_t *h, double dloss, double *grad_tau, double *grad_
     // per segment) when graphs are on and the copy buffer fits.
     ADJ_CUDA(prepare_adjoint2(h));
     const int nck = (T + c - 1) / c;
-    bool graphs = h->graph_iters > 1 && c >= 2 && (int)s.seg.size() >= c - 1;
-    if (graphs && s.seg_graph_c != c) {  // graphs of another segment length
+    bool graphs = h->graph_iters > 1 && c >= 2 && (macro || (int)s.seg.size() >= c - 1);
+    if (graphs && (s.seg_graph_c != c || s.seg_graph_macro != macro)) {  // graphs of another sweep
         drop_segment_graphs(s);
         s.seg_graph_c = c;
+        s.seg_graph_macro = macro;
     }
     if (graphs && !s.q0) {
-        size_t freeb = 0, totalb = 0;
-        ADJ_CUDA(cudaMemGetInfo(&freeb, &totalb));
-        const size_t cap = h->cfg.max_device_bytes;
-        const bool fits = freeb > fbytes + ((size_t)1 << 30) &&
-                          (cap == 0 || h->base_bytes + s.bytes + fbytes <= cap);
-        if (!fits || alloc_tracked(h, &s.q0, fbytes) != LBM_OK) graphs = false;
+        if (room() < fbytes || alloc_tracked(h, &s.q0, fbytes) != LBM_OK) graphs = false;
     }
     for (int j = nck - 1; j >= 0; --j) {
         const int start = j * c, len = std::min(T, start + c) - start;
         if (graphs && len == c) {
             ADJ_CUDA(cudaMemcpyAsync(s.q0, s.ckpt[j], fbytes, cudaMemcpyDeviceToDevice, st));
-            const int rc = replay_segment(h, c, cur);
+            const int rc = replay_segment(h, c, cur, macro);
             if (rc != LBM_OK) return rc;
             continue;
         }
-        const int rc = sweep(h, s.ckpt[j], start, len, s.seg, 0, (int)s.seg.size(), cur);
+        const int rc = macro ? sweep_macro(h, s.ckpt[j], start, len, cur)
+                             : sweep(h, s.ckpt[j], start, len, s.seg, 0, (int)s.seg.size(), cur);
         if (rc != LBM_OK) return rc;
     }
     // a_0 = dJ/dR_0; the init kernel's lid dependence of R_0
@@ -646,16 +749,17 @@ int lbm_adjoint_backward(lbm_t *h, double dloss, double *grad_tau, double *grad_
         for (size_t o0 = 0; o0 < total; o0 += chunk) {
             const size_t cnt = std::min(chunk, total - o0);
             const unsigned g = (unsigned)((cnt + 255) / 256);
-            if (ab == 8)
-                lbm::export_adjoint_kernel<double><<<g, 256, 0, st>>>(static_cast<const double *>(s.adj[cur]),
-                                                                       static_cast<double *>(h->stage), o0, cnt,
-                                                                       h->sd, h->n);
+            if (ab == 8 && db == 8)
+                lbm::export_adjoint_kernel<double, double><<<g, 256, 0, st>>>(
+                    static_cast<const double *>(s.adj[cur]), static_cast<double *>(h->stage), o0, cnt, h->sd, h->n);
+            else if (ab == 8)
+                lbm::export_adjoint_kernel<double, float><<<g, 256, 0, st>>>(
+                    static_cast<const double *>(s.adj[cur]), static_cast<float *>(h->stage), o0, cnt, h->sd, h->n);
             else
-                lbm::export_adjoint_kernel<float><<<g, 256, 0, st>>>(static_cast<const float *>(s.adj[cur]),
-                                                                      static_cast<float *>(h->stage), o0, cnt,
-                                                                      h->sd, h->n);
+                lbm::export_adjoint_kernel<float, float><<<g, 256, 0, st>>>(
+                    static_cast<const float *>(s.adj[cur]), static_cast<float *>(h->stage), o0, cnt, h->sd, h->n);
             ADJ_CUDA(cudaGetLastError());
-            ADJ_CUDA(cudaMemcpyAsync((char *)grad_f0 + o0 * ab, h->stage, cnt * ab, cudaMemcpyDeviceToHost, st));
+            ADJ_CUDA(cudaMemcpyAsync((char *)grad_f0 + o0 * db, h->stage, cnt * db, cudaMemcpyDeviceToHost, st));
         }
     }
     ADJ_CUDA(cudaEventRecord(h->ev_last, st));

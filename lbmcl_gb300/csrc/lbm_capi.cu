@@ -223,7 +223,7 @@ int setup_staged(lbm_t *h, int want_stages)
 
 cudaError_t launch_pull(const lbm_t *h, int mode, const lbm::StepArgs &a, unsigned *nparts = nullptr)
 {
-    if (h->kernel == LBM_KERNEL_STAGED && mode != lbm::MODE_REDUCE) {
+    if (h->kernel == LBM_KERNEL_STAGED && (mode == lbm::MODE_STEP || mode == lbm::MODE_STEP_MACRO)) {
         switch (h->prec) {
         case LBM_FP32: return lbm::launch_staged_f32(mode, a, h->sgrid, h->sblock, h->ssmem, h->stream);
         case LBM_FP64: return lbm::launch_staged_f64(mode, a, h->sgrid, h->sblock, h->ssmem, h->stream);
@@ -296,6 +296,16 @@ cudaError_t launch_iteration(const lbm_t *h, const void *fin, void *fout)
     a.fout = fout;
     return launch_pull(h, MODE_STEP, a);
 }
+
+cudaError_t launch_iteration_adj(const lbm_t *h, const void *fin, void *fout, void *point)
+{
+    StepArgs a = step_args(h, h->cur);
+    a.fin = fin;
+    a.fout = fout;
+    a.rho = nullptr;
+    a.u = point;
+    return launch_pull(h, MODE_STEP_ADJ, a);
+}
 }  // namespace lbm
 
 extern "C" {
@@ -363,6 +373,10 @@ int lbm_init(lbm_t **out, const lbm_config *c)
         return fail(LBM_EINVAL, "lbm_init: adjoint_steps %d out of range (0, 1, 2)", c->adjoint_steps);
     if (c->adjoint_max_states < 0)
         return fail(LBM_EINVAL, "lbm_init: adjoint_max_states %d must be >= 0", c->adjoint_max_states);
+    if (c->adjoint_fp64 < 0 || c->adjoint_fp64 > 1)
+        return fail(LBM_EINVAL, "lbm_init: adjoint_fp64 %d must be 0 or 1", c->adjoint_fp64);
+    if (c->adjoint_full_states < 0 || c->adjoint_full_states > 1)
+        return fail(LBM_EINVAL, "lbm_init: adjoint_full_states %d must be 0 or 1", c->adjoint_full_states);
     if (c->graph_iterations < 0 || c->graph_iterations > 256 || (c->graph_iterations > 1 && c->graph_iterations % 2))
         return fail(LBM_EINVAL, "lbm_init: graph_iterations %d must be 0, 1 or an even number <= 256",
                     c->graph_iterations);

@@ -288,8 +288,10 @@ __device__ __forceinline__ float deq_scaled(int i, float drho, float rho, float 
 }
 
 // Pull-kernel variants: plain iteration, iteration that also stores rho/u,
-// and moments-only pass that writes FP64 reduction partials.
-enum { MODE_STEP = 0, MODE_STEP_MACRO = 1, MODE_REDUCE = 2 };
+// moments-only pass that writes FP64 reduction partials, and iteration that
+// stores the adjoint's linearisation point of its input (three planes at
+// StepArgs::u: u_x, u_y, u_z of FLUID sites; rho, 0, 0 of MOVING sites).
+enum { MODE_STEP = 0, MODE_STEP_MACRO = 1, MODE_REDUCE = 2, MODE_STEP_ADJ = 3 };
 
 // ---------------------------------------------------------------------------
 // Per-launch parameters.

@@ -34,6 +34,11 @@ struct lbm_adjoint_state {
     cudaGraphExec_t seg_exec[2] = {nullptr, nullptr};
     int seg_flip[2] = {0, 0};
     int seg_graph_c = 0;
+    bool seg_graph_macro = false;  // the graphs are of the stored-point sweep
+    // stored-point sweep (no tau gradient): the linearisation point of every
+    // iteration of one segment (3 planes each) and two state scratch buffers
+    std::vector<void *> mseg;
+    void *mtmp[2] = {nullptr, nullptr};
 };
 
 struct lbm_handle {
@@ -104,6 +109,9 @@ inline size_t storage_bytes(int prec) { return prec == LBM_FP64 ? 8 : (prec == L
 inline size_t macro_bytes(int prec) { return prec == LBM_FP64 ? 8 : 4; }
 // launch one iteration P_out = C(S(P_in)) with the handle's kernel variant
 cudaError_t launch_iteration(const lbm_t *h, const void *fin, void *fout);
+// the same iteration, also storing the adjoint's linearisation point of its
+// input (MODE_STEP_ADJ: three planes of the compute type at `point`)
+cudaError_t launch_iteration_adj(const lbm_t *h, const void *fin, void *fout, void *point);
 // h->graph_iters iterations from h->f[h->cur] as one replayed CUDA graph
 // (an even count: h->cur is unchanged)
 cudaError_t replay_iterations(lbm_t *h);

@@ -224,9 +224,10 @@ __device__ __forceinline__ void relax_pair_dev(float &dp, float &dm, float a, in
     dm = __fmaf_rn(K.keep, dm, __fmaf_rn(K.k[c], X, -lin));
 }
 
-// FLUID site in deviation form.
-template <bool COLLIDE>
-__device__ __forceinline__ void fluid_dev(float (&D)[Q], const DevK &K, SiteOut &o)
+// Moments of a FLUID site in deviation form (D = s (f - w)): drho = rho - 1,
+// rho, u; the forward's own arithmetic, also the adjoint's linearisation point.
+__device__ __forceinline__ void moments_dev(const float (&D)[Q], float inv_s, float &drho, float &rho, float &ux,
+                                            float &uy, float &uz)
 {
     const float s13 = __fadd_rn(D[1], D[3]), d13 = __fsub_rn(D[1], D[3]);
     const float s24 = __fadd_rn(D[2], D[4]), d24 = __fsub_rn(D[2], D[4]);
@@ -243,10 +244,20 @@ __device__ __forceinline__ void fluid_dev(float (&D)[Q], const DevK &K, SiteOut 
     const float jx = __fadd_rn(__fsub_rn(__fadd_rn(d13, d79), d810), __fadd_rn(d1117, d1513));
     const float jy = __fadd_rn(__fadd_rn(__fadd_rn(d24, d79), d810), __fadd_rn(d1218, d1614));
     const float jz = __fadd_rn(__fsub_rn(__fsub_rn(d65, d1117), d1218), __fadd_rn(d1513, d1614));
-    const float drho = __fmul_rn(sd, K.inv_s);
-    const float rho = __fadd_rn(1.0f, drho);
-    const float kk = __fmul_rn(K.inv_s, __fdividef(1.0f, rho));
-    const float ux = __fmul_rn(jx, kk), uy = __fmul_rn(jy, kk), uz = __fmul_rn(jz, kk);
+    drho = __fmul_rn(sd, inv_s);
+    rho = __fadd_rn(1.0f, drho);
+    const float kk = __fmul_rn(inv_s, __fdividef(1.0f, rho));
+    ux = __fmul_rn(jx, kk);
+    uy = __fmul_rn(jy, kk);
+    uz = __fmul_rn(jz, kk);
+}
+
+// FLUID site in deviation form.
+template <bool COLLIDE>
+__device__ __forceinline__ void fluid_dev(float (&D)[Q], const DevK &K, SiteOut &o)
+{
+    float drho, rho, ux, uy, uz;
+    moments_dev(D, K.inv_s, drho, rho, ux, uy, uz);
     o.macro = true;
     o.bad = !(rho > 0.0f);
     o.r = rho; o.ux = ux; o.uy = uy; o.uz = uz;
@@ -377,6 +388,49 @@ __device__ __forceinline__ void store_macro(const StepArgs &a, size_t id, const 
     u[2 * a.n + id] = (C)o.uz;
 }
 
+// The adjoint's linearisation point of one site (MODE_STEP_ADJ): u of a
+// FLUID site, rho (then 0, 0) of a MOVING site, in the three planes at a.u.
+template <class C>
+__device__ __forceinline__ void store_adj(const StepArgs &a, size_t id, const SiteOut &o, bool moving)
+{
+    C *u = static_cast<C *>(a.u);
+    u[id] = moving ? (C)o.r : (C)o.ux;
+    u[a.n + id] = (C)o.uy;
+    u[2 * a.n + id] = (C)o.uz;
+}
+
+// rho / u (MODE_STEP_MACRO) or the FLUID linearisation point (MODE_STEP_ADJ)
+// of two neighbouring FLUID-or-not sites (id even) with one 2-element vector
+// store per field when both store, else per site
+template <class C> struct Vec2;
+template <> struct Vec2<float> { using type = float2; };
+template <> struct Vec2<double> { using type = double2; };
+template <class C, int MODE>
+__device__ __forceinline__ void store_macro_pair(const StepArgs &a, size_t id, bool s0, bool s1, const SiteOut &o0,
+                                                 const SiteOut &o1)
+{
+    static_assert(MODE == MODE_STEP_MACRO || MODE == MODE_STEP_ADJ, "storing modes");
+    if (s0 && s1) {
+        using V2 = typename Vec2<C>::type;
+        C *u = static_cast<C *>(a.u);
+        if (MODE == MODE_STEP_MACRO) {
+            C *rho = static_cast<C *>(a.rho);
+            *reinterpret_cast<V2 *>(rho + id) = V2{(C)o0.r, (C)o1.r};
+        }
+        *reinterpret_cast<V2 *>(u + id) = V2{(C)o0.ux, (C)o1.ux};
+        *reinterpret_cast<V2 *>(u + a.n + id) = V2{(C)o0.uy, (C)o1.uy};
+        *reinterpret_cast<V2 *>(u + 2 * a.n + id) = V2{(C)o0.uz, (C)o1.uz};
+        return;
+    }
+    if (MODE == MODE_STEP_MACRO) {
+        if (s0) store_macro<C>(a, id, o0);
+        if (s1) store_macro<C>(a, id + 1, o1);
+    } else {
+        if (s0) store_adj<C>(a, id, o0, false);
+        if (s1) store_adj<C>(a, id + 1, o1, false);
+    }
+}
+
 __device__ __forceinline__ void accumulate(const SiteOut &o, double &m, double &e)
 {
     m += o.r;
@@ -419,6 +473,7 @@ __device__ __forceinline__ void update_general(S (&fs)[Q][V], typename MapWord<V
         }
         bad |= o.bad;
         if (MODE == MODE_STEP_MACRO && o.macro) store_macro<C>(a, site0 + k, o);
+        if (MODE == MODE_STEP_ADJ && o.macro) store_adj<C>(a, site0 + k, o, b != 0);
         if (MODE == MODE_REDUCE && o.macro) accumulate(o, red_m, red_e);
     }
     if (bad) atomicOr(a.status, 1);
@@ -442,19 +497,26 @@ __device__ __forceinline__ void update_vector(S (&fs)[Q][V], typename MapWord<V>
     if constexpr (!DEV) {
         if (FLUID_ONLY) {
 #pragma unroll
-            for (int k = 0; k < V; ++k) {
-                C f[Q];
+            for (int k = 0; k < V; k += 2) {
+                SiteOut o[2];
 #pragma unroll
-                for (int i = 0; i < Q; ++i) f[i] = fs[i][k];
-                SiteOut o;
-                site_exact<C, MODE != MODE_REDUCE>(f, 0, (C)0, inv_tau, W, o);
+                for (int h = 0; h < 2; ++h) {
+                    C f[Q];
 #pragma unroll
-                for (int i = 0; i < Q; ++i) fs[i][k] = f[i];
+                    for (int i = 0; i < Q; ++i) f[i] = fs[i][k + h];
+                    site_exact<C, MODE != MODE_REDUCE>(f, 0, (C)0, inv_tau, W, o[h]);
+#pragma unroll
+                    for (int i = 0; i < Q; ++i) fs[i][k + h] = f[i];
+                }
                 // x in [2, dim-3] is FLUID; the row ends are walls / faces
-                if ((unsigned)(x0 + k - 2) <= (unsigned)(dim - 5)) {
-                    bad |= o.bad;
-                    if (MODE == MODE_STEP_MACRO) store_macro<C>(a, site0 + k, o);
-                    if (MODE == MODE_REDUCE) accumulate(o, red_m, red_e);
+                const bool f0 = (unsigned)(x0 + k - 2) <= (unsigned)(dim - 5);
+                const bool f1 = (unsigned)(x0 + k - 1) <= (unsigned)(dim - 5);
+                bad |= (f0 && o[0].bad) || (f1 && o[1].bad);
+                if constexpr (MODE == MODE_STEP_MACRO || MODE == MODE_STEP_ADJ)
+                    store_macro_pair<C, MODE>(a, site0 + k, f0, f1, o[0], o[1]);
+                if (MODE == MODE_REDUCE) {
+                    if (f0) accumulate(o[0], red_m, red_e);
+                    if (f1) accumulate(o[1], red_m, red_e);
                 }
             }
             if (bad) atomicOr(a.status, 1);
@@ -484,10 +546,8 @@ __device__ __forceinline__ void update_vector(S (&fs)[Q][V], typename MapWord<V>
                 const bool f0 = !FLUID_ONLY || (unsigned)(x0 + k - 2) <= (unsigned)(dim - 5);
                 const bool f1 = !FLUID_ONLY || (unsigned)(x0 + k - 1) <= (unsigned)(dim - 5);
                 bad |= (f0 && o0.bad) || (f1 && o1.bad);
-                if (MODE == MODE_STEP_MACRO) {
-                    if (f0) store_macro<C>(a, site0 + k, o0);
-                    if (f1) store_macro<C>(a, site0 + k + 1, o1);
-                }
+                if constexpr (MODE == MODE_STEP_MACRO || MODE == MODE_STEP_ADJ)
+                    store_macro_pair<C, MODE>(a, site0 + k, f0, f1, o0, o1);
                 if (MODE == MODE_REDUCE) {
                     if (f0) accumulate(o0, red_m, red_e);
                     if (f1) accumulate(o1, red_m, red_e);
@@ -859,14 +919,17 @@ __device__ __forceinline__ C lid_at(const InitArgs &a, int x, int y)
     return static_cast<const C *>(a.lid)[(size_t)y * a.dim + x];
 }
 
+// Grid: blockIdx.y = z-plane, x-blocks over the dim^2 sites of the plane
+// (32-bit index arithmetic inside a plane).
 template <class S>
 __global__ void init_kernel(InitArgs a)
 {
     using C = typename Compute<S>::type;
-    const size_t id = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (id >= a.n) return;
     const int dim = a.dim;
-    const int x = (int)(id % dim), y = (int)((id / dim) % dim), z = (int)(id / ((size_t)dim * dim));
+    const unsigned pi = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pi >= (unsigned)dim * (unsigned)dim) return;
+    const int x = (int)(pi % (unsigned)dim), y = (int)(pi / (unsigned)dim), z = (int)blockIdx.y;
+    const size_t id = (size_t)z * dim * dim + pi;
     const uint8_t b = pack_cell(dim, x, y, z);
     a.map[id] = b;
     const bool store = (b == 0) || (b == M_FRONT);
@@ -887,22 +950,18 @@ __global__ void init_kernel(InitArgs a)
             const int tx = x + ex_of(i), ty = y + ey_of(i), tz = z + ez_of(i);
             const uint8_t tb = pack_cell(dim, tx, ty, tz);
             if (!(tb & M_WALL)) {
-                const size_t tid = (size_t)tx + (size_t)ty * dim + (size_t)tz * dim * dim;
                 const C lv = (tb & M_FRONT) ? lid_at<C>(a, tx, ty) : (C)0;
                 if constexpr (is_dev16<S>()) {
-                    // deviation of the equilibrium at rho = 1, plus noise
+                    // deviation of the equilibrium at rho = 1 (the noise of
+                    // FLUID targets is written by noise_kernel)
                     float d = 0.0f;
                     if (tb & M_FRONT) {
                         const float eu = ex_of(i) > 0 ? (float)lv : (ex_of(i) < 0 ? -(float)lv : 0.0f);
                         d = deq_scaled(i, 0.0f, 1.0f, eu, 1.5f * (float)lv * (float)lv, 1.0f);
                     }
-                    if (a.noise_sigma != 0.0 && tb == 0)
-                        d = d + (float)__dmul_rn(a.noise_sigma, (double)gauss(a.seed, tid, (uint32_t)i));
                     val = d * Dev16<S>::scale;
                 } else {
                     val = (tb & M_FRONT) ? init_eq_exact<C>(i, lv, W) : W.w[wclass_of(i)];
-                    if (a.noise_sigma != 0.0 && tb == 0)
-                        val = X<C>::add(val, (C)__dmul_rn(a.noise_sigma, (double)gauss(a.seed, tid, (uint32_t)i)));
                 }
             }
         }
@@ -910,6 +969,44 @@ __global__ void init_kernel(InitArgs a)
             f[(size_t)i * a.n + id] = Dev16<S>::from_f((float)val);
         } else {
             f[(size_t)i * a.n + id] = (S)val;
+        }
+    }
+}
+
+// Seeded N(0, sigma^2) noise on the initial populations of the FLUID sites
+// (x, y, z in [2, dim-3]), run after init_kernel: the thread of FLUID site t
+// draws its ten sample pairs (populations 2m, 2m+1 <- pair m) and writes the
+// 19 slots (t - e_q, q) of P_{-1} that stream into t, each slot having this
+// one writer: the equilibrium at rest (w_q; deviation 0) plus sigma z.
+template <class S>
+__global__ void noise_kernel(InitArgs a)
+{
+    using C = typename Compute<S>::type;
+    const int dim = a.dim;
+    const unsigned m = (unsigned)(dim - 4);
+    const unsigned k = blockIdx.x * blockDim.x + threadIdx.x;  // grid: blockIdx.y = z - 2
+    if (k >= m * m) return;
+    const size_t x = 2 + k % m, y = 2 + k / m, z = 2 + (size_t)blockIdx.y;
+    const size_t t = x + y * (size_t)dim + z * (size_t)dim * dim;
+    S *f = static_cast<S *>(a.f);
+    const Weights<C> W = make_weights<C>();
+#pragma unroll
+    for (int p = 0; p < (Q + 1) / 2; ++p) {
+        float z0, z1;
+        gauss_pair(a.seed, t, (uint32_t)p, z0, z1);
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int q = 2 * p + h;
+            if (q >= Q) break;
+            const double sz = __dmul_rn(a.noise_sigma, (double)(h ? z1 : z0));
+            const ptrdiff_t sh = (ptrdiff_t)ex_of(q) + (ptrdiff_t)ey_of(q) * dim + (ptrdiff_t)ez_of(q) * dim * dim;
+            S *dst = f + (size_t)q * a.n + (size_t)((ptrdiff_t)t - sh);
+            if constexpr (is_dev16<S>()) {
+                const float val = __fmul_rn((float)sz, Dev16<S>::scale);
+                *dst = Dev16<S>::from_f(val);
+            } else {
+                *dst = (S)X<C>::add(W.w[wclass_of(q)], (C)sz);
+            }
         }
     }
 }

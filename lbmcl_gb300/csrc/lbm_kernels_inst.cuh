@@ -32,6 +32,7 @@ static cudaError_t launch_direct(int mode, const StepArgs &a0, unsigned block, c
                 pull_kernel<LBM_S, MODE_STEP_MACRO, VB, ROWS_INTERIOR><<<grid, block, 0, s>>>(a);
                 break;
             case MODE_REDUCE: pull_kernel<LBM_S, MODE_REDUCE, VB, ROWS_INTERIOR><<<grid, block, 0, s>>>(a); break;
+            case MODE_STEP_ADJ: pull_kernel<LBM_S, MODE_STEP_ADJ, VB, ROWS_INTERIOR><<<grid, block, 0, s>>>(a); break;
             default: return cudaErrorInvalidValue;
             }
         } else {
@@ -39,6 +40,7 @@ static cudaError_t launch_direct(int mode, const StepArgs &a0, unsigned block, c
             case MODE_STEP: pull_kernel<LBM_S, MODE_STEP, VB, ROWS_FACES><<<grid, block, 0, s>>>(a); break;
             case MODE_STEP_MACRO: pull_kernel<LBM_S, MODE_STEP_MACRO, VB, ROWS_FACES><<<grid, block, 0, s>>>(a); break;
             case MODE_REDUCE: pull_kernel<LBM_S, MODE_REDUCE, VB, ROWS_FACES><<<grid, block, 0, s>>>(a); break;
+            case MODE_STEP_ADJ: pull_kernel<LBM_S, MODE_STEP_ADJ, VB, ROWS_FACES><<<grid, block, 0, s>>>(a); break;
             default: return cudaErrorInvalidValue;
             }
         }
@@ -89,8 +91,12 @@ const void *LBM_CAT(staged_kernel_ptr_, LBM_SFX)(int mode)
 cudaError_t LBM_CAT(launch_init_, LBM_SFX)(const InitArgs &a, cudaStream_t s)
 {
     const unsigned block = 256;
-    const size_t grid = (a.n + block - 1) / block;
-    init_kernel<LBM_S><<<(unsigned)grid, block, 0, s>>>(a);
+    const dim3 grid((unsigned)(((size_t)a.dim * a.dim + block - 1) / block), (unsigned)a.dim);
+    init_kernel<LBM_S><<<grid, block, 0, s>>>(a);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess || a.noise_sigma == 0.0 || a.dim < 5) return e;
+    const size_t m = (size_t)(a.dim - 4);
+    noise_kernel<LBM_S><<<dim3((unsigned)((m * m + block - 1) / block), (unsigned)m), block, 0, s>>>(a);
     return cudaGetLastError();
 }
 

@@ -1,13 +1,17 @@
 // lbm_noise.cuh -- seeded Gaussian perturbation of the initial populations.
 //
-// N(0,1) sample for (seed, site, q): Philox4x32-10 (Salmon, Moraes, Dror,
-// Shaw, SC'11) on the counter (site_lo, site_hi, q, block), two 24-bit
-// uniform pairs per block, Marsaglia's polar method, and a natural logarithm
-// summed from the atanh series.  Every floating-point step is an explicit
-// IEEE single-precision operation (no contraction, no library
-// transcendental), so a CPU implementation of the same recipe gets the same
-// bits.  Single precision because FP64 runs at a small fraction of the FP32
-// rate on GB300 and the samples only perturb the initial state.
+// Two N(0,1) samples per (seed, site, pair): Philox4x32-10 (Salmon, Moraes,
+// Dror, Shaw, SC'11) on the counter (site_lo, site_hi, pair, block); each
+// 32-bit output word is one attempt of Marsaglia's polar method (its low and
+// high 16 bits give the uniform pair), so one block offers four attempts and
+// a warp rarely needs a second block; an accepted attempt gives both
+// normals.  Populations 2m and 2m+1 of a site take the two samples of pair m.
+// The natural logarithm is summed from the atanh series.  Every
+// floating-point step is an explicit IEEE single-precision operation (no
+// contraction, no library transcendental), so a CPU implementation of the
+// same recipe gets the same bits.  Single precision because FP64 runs at a
+// small fraction of the FP32 rate on GB300 and the samples only perturb the
+// initial state.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -64,30 +68,42 @@ __device__ __forceinline__ float series_logf(float x)
     return __fadd_rn(__fmul_rn((float)e, ln2), __fmul_rn(__fmul_rn(2.0f, s), acc));
 }
 
-__device__ __forceinline__ float sym_uniform(uint32_t a)
+// uniform in (-1, 1) from 16 random bits: (a + 1/2) / 2^15 - 1, exact
+__device__ __forceinline__ float sym_uniform16(uint32_t a)
 {
-    const float u01 = __fmul_rn(__fadd_rn((float)(a >> 8), 0.5f), 1.0f / 16777216.0f);
-    return __fsub_rn(__fmul_rn(2.0f, u01), 1.0f);
+    return __fsub_rn(__fmul_rn(__fadd_rn((float)a, 0.5f), 1.0f / 32768.0f), 1.0f);
 }
 
-// Marsaglia polar method; each Philox block gives two attempts (32 blocks at most).
-__device__ __forceinline__ float gauss(uint64_t seed, uint64_t site, uint32_t q)
+// The two samples of pair `pair` of a site (at most 64 attempts).
+__device__ __forceinline__ void gauss_pair(uint64_t seed, uint64_t site, uint32_t pair, float &z0, float &z1)
 {
     const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
-    for (uint32_t block = 0; block < 32; ++block) {
-        uint32_t c[4] = {(uint32_t)site, (uint32_t)(site >> 32), q, block};
+    for (uint32_t block = 0; block < 16; ++block) {
+        uint32_t c[4] = {(uint32_t)site, (uint32_t)(site >> 32), pair, block};
         philox4x32_10(c, k0, k1);
 #pragma unroll
-        for (int half = 0; half < 2; ++half) {
-            const float v1 = sym_uniform(c[2 * half]);
-            const float v2 = sym_uniform(c[2 * half + 1]);
+        for (int a = 0; a < 4; ++a) {
+            const float v1 = sym_uniform16(c[a] & 0xffffu);
+            const float v2 = sym_uniform16(c[a] >> 16);
             const float s = __fadd_rn(__fmul_rn(v1, v1), __fmul_rn(v2, v2));
             if (s >= 1.0f || s == 0.0f) continue;
             const float t = __fdiv_rn(__fmul_rn(-2.0f, series_logf(s)), s);
-            return __fmul_rn(v1, __fsqrt_rn(t));
+            const float r = __fsqrt_rn(t);
+            z0 = __fmul_rn(v1, r);
+            z1 = __fmul_rn(v2, r);
+            return;
         }
     }
-    return 0.0f;
+    z0 = 0.0f;
+    z1 = 0.0f;
+}
+
+// The sample of population q of a site.
+__device__ __forceinline__ float gauss(uint64_t seed, uint64_t site, uint32_t q)
+{
+    float z0, z1;
+    gauss_pair(seed, site, q >> 1, z0, z1);
+    return (q & 1u) ? z1 : z0;
 }
 
 }  // namespace lbm

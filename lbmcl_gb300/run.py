@@ -28,6 +28,7 @@ def main(argv=None) -> int:
     ap.add_argument("--adjoint-max-states", type=int, default=0, help="cap on the backward sweep's state buffers")
     ap.add_argument("--adjoint", default="", help="T,c: also run an adjoint forward/backward of T iterations, "
                                                   "checkpoint every c")
+    ap.add_argument("--tau", action="store_true", help="the adjoint also forms dJ/dtau (full-state segments)")
     a = ap.parse_args(argv)
     with capi.Lattice(a.dim, a.viscosity, a.velocity, precision=a.precision, stride=0, seed=a.seed,
                       noise_sigma=a.noise, block_threads=a.block, profile_steps=True, kernel=a.kernel,
@@ -45,10 +46,11 @@ def main(argv=None) -> int:
             t0 = time.perf_counter()
             J = L.adjoint_forward(T, c)
             t1 = time.perf_counter()
-            g_tau, g_lid, _ = L.adjoint_backward(1.0, want_f0=False)
+            g_tau, g_lid, _ = L.adjoint_backward(1.0, want_f0=False, want_tau=a.tau)
             t2 = time.perf_counter()
             print(f"adjoint T={T} c={c} loss={J:.6e} forward={1e3 * (t1 - t0) / T:.4f} ms/iter "
-                  f"backward={1e3 * (t2 - t1) / T:.4f} ms/iter dJ/dtau={g_tau:.6e}")
+                  f"backward={1e3 * (t2 - t1) / T:.4f} ms/iter |dJ/dlid|={float((g_lid ** 2).sum()) ** 0.5:.6e}"
+                  + (f" dJ/dtau={g_tau:.6e}" if a.tau else ""))
     wet = (a.dim - 2) ** 3
     print(f"dim={a.dim} precision={a.precision} steps={a.steps} kernels={kernels_ms:.3f} ms "
           f"kernel MLUPS={wet * a.steps / (kernels_ms * 1e3):.1f} wall={wall * 1e3:.1f} ms "

@@ -16,9 +16,13 @@ adjoint   64^3, nu = 0.01: loss = mid-plane u_x MSE against the field of a
 lidfield  256^3, nu = 0.0089: per-column lid field 0.05 + N(0, 0.005); target
           made by a forward run with a smooth lid (4 random 2-D sinusoids of
           total amplitude 0.02 around 0.05); 16-bit forward, FP32 adjoint,
-          sqrt checkpointing.  Adjoint/forward time, device memory, gradient
-          error against FP64 finite differences on random active columns and
-          against the FP64 adjoint.
+          sqrt checkpointing.  Adjoint/forward time, device memory, and the
+          gradient's error budget on random active columns: the FP32
+          adjoint's rounding (against the FP64 adjoint of the same 16-bit
+          trajectory), the storage rounding it linearises through (against
+          central differences of the 16-bit model), the model difference
+          (against the FP64 model's adjoint) and the FP64 adjoint's exactness
+          (against FP64 central differences).
 Each prints one JSON object.  Every run uses the GPU library only.
 """
 from __future__ import annotations
@@ -178,6 +182,20 @@ def smooth_lid(dim, rng, amplitude=0.02, base=0.05):
 
 
 def lidfield(args):
+    """The 256^3 x 10000 lid-field gradient and its error budget.
+
+    g_32   FP32 adjoint of the 16-bit trajectory (the product; lid control,
+           stored-point sweep)
+    g_a64  FP64-arithmetic adjoint of the same 16-bit trajectory
+    fd16   central differences of the 16-bit model itself, h well above the
+           FP16 quantum of the stored deviations, three h halving, Richardson
+           extrapolated (FD(h) = g + c h^2 + rounding noise / h)
+    g_64   FP64 adjoint of the FP64 trajectory (the FP64 model)
+    fd64   FP64 central differences (h = 1e-6) of the FP64 model
+    Components: (i) adjoint rounding |g_32 - g_a64|; (ii) linearisation of
+    the storage rounding |g_a64 - fd16|; (iii) the model difference
+    |g_a64 - g_64|; and the exactness |g_64 - fd64| of the FP64 adjoint.
+    """
     import torch
     dim, steps, c = args.dim, args.steps, args.every
     nu = 0.0089
@@ -190,8 +208,11 @@ def lidfield(args):
         L.step(1, every=steps + 1)
         target = np.nan_to_num(L.u().reshape(3, dim, dim, dim)[0, :, plane, :]).reshape(-1)
     lid = 0.05 + 0.005 * rng.standard_normal(dim * dim)
+    cols = [(int(a), int(b)) for a, b in rng.integers(2, dim - 2, size=(args.columns, 2))]
+    act = (slice(2, dim - 2), slice(2, dim - 2))
     out = {"check": "lidfield", "dim": dim, "steps": steps, "checkpoint_every": c, "nu": nu, "plane_y": plane,
-           "storage": args.precision, "adjoint": "fp32"}
+           "storage": args.precision, "adjoint": "fp32", "control": "per-column lid field",
+           "columns": [{"x": x, "y": y} for x, y in cols]}
     with capi.Lattice(dim, velocity=0.0, precision=args.precision, lid=lid, tau=tau, stride=0) as L:
         stream = torch.cuda.ExternalStream(L.stream)
         L.step(3)
@@ -202,56 +223,78 @@ def lidfield(args):
         e1.record(stream)
         e1.synchronize()
         fwd_ms = e0.elapsed_time(e1) / 100
-    free0, total = torch.cuda.mem_get_info()
-    with capi.Lattice(dim, velocity=0.0, precision=args.precision, lid=lid, tau=tau, stride=0) as L:
-        L.adjoint_set_loss(plane, target)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        J = L.adjoint_forward(steps, c)
-        t1 = time.perf_counter()
-        free1, _ = torch.cuda.mem_get_info()
-        gt, gl, _ = L.adjoint_backward(1.0, want_f0=False)
-        t2 = time.perf_counter()
-        free2, _ = torch.cuda.mem_get_info()
-    out.update({"loss": J, "forward_ms_per_iter": round(fwd_ms, 4),
-                "checkpointed_forward_ms_per_iter": round((t1 - t0) * 1e3 / steps, 4),
-                "backward_ms_per_iter": round((t2 - t1) * 1e3 / steps, 4),
-                "adjoint_over_forward": round((t2 - t1) * 1e3 / steps / fwd_ms, 3),
-                "device_gb_used_peak": round((free0 - min(free1, free2)) / 1e9, 2)})
-    if args.fp64_adjoint:
-        # FP64 states are 4x the 16-bit ones: wider top-level checkpoints, and
-        # the backward sweep checkpoints each segment again as memory requires
-        c64 = args.fp64_every
-        free_a, _ = torch.cuda.mem_get_info()
-        with capi.Lattice(dim, velocity=0.0, precision="fp64", lid=lid, tau=tau, stride=0) as L:
+
+    def run_adjoint(prec, every, a64=False):
+        free0, _ = torch.cuda.mem_get_info()
+        with capi.Lattice(dim, velocity=0.0, precision=prec, lid=lid, tau=tau, stride=0, adjoint_fp64=a64) as L:
             L.adjoint_set_loss(plane, target)
+            torch.cuda.synchronize()
             t0 = time.perf_counter()
-            J64 = L.adjoint_forward(steps, c64)
+            J = L.adjoint_forward(steps, every)
             t1 = time.perf_counter()
-            gt64, gl64, _ = L.adjoint_backward(1.0, want_f0=False)
+            free1, _ = torch.cuda.mem_get_info()
+            _, gl, _ = L.adjoint_backward(1.0, want_f0=False, want_tau=False)
             t2 = time.perf_counter()
-            free_b, _ = torch.cuda.mem_get_info()
-        act = (slice(2, dim - 2), slice(2, dim - 2))
-        out["fp64_adjoint_run"] = {"checkpoint_every": c64, "forward_s": round(t1 - t0, 1),
-                                   "backward_s": round(t2 - t1, 1),
-                                   "device_gb_used": round((free_a - free_b) / 1e9, 1)}
-        out["vs_fp64_adjoint"] = {"loss_fp64": J64,
-                                  "lid_rel_l2": float(np.linalg.norm(gl[act] - gl64[act]) / np.linalg.norm(gl64[act])),
-                                  "tau_rel": abs(gt - gt64) / abs(gt64)}
-    h = 1e-6
-    rows = []
-    for (x, y) in [(int(a), int(b)) for a, b in rng.integers(2, dim - 2, size=(args.columns, 2))]:
-        lp, lm = lid.copy(), lid.copy()
-        lp[x + y * dim] += h
-        lm[x + y * dim] -= h
-        d = (_loss(dim, steps, lp, tau, plane, target, "fp64", stride=0) -
-             _loss(dim, steps, lm, tau, plane, target, "fp64", stride=0)) / (2 * h)
-        row = {"x": x, "y": y, "fd_fp64": d, "adjoint": float(gl[y, x]), "rel": abs(gl[y, x] - d) / abs(d)}
-        if args.fp64_adjoint:
-            row["adjoint_fp64"] = float(gl64[y, x])
-            row["rel_fp64"] = abs(gl64[y, x] - d) / abs(d)
-        rows.append(row)
-    out["finite_differences_fp64_h1e-6"] = rows
+            free2, _ = torch.cuda.mem_get_info()
+        return J, gl, t1 - t0, t2 - t1, (free0 - min(free1, free2)) / 1e9
+
+    J, g32, tf, tb, gb = run_adjoint(args.precision, c)
+    out.update({"loss": J, "forward_ms_per_iter": round(fwd_ms, 4),
+                "checkpointed_forward_ms_per_iter": round(tf * 1e3 / steps, 4),
+                "backward_ms_per_iter": round(tb * 1e3 / steps, 4),
+                "adjoint_over_forward": round(tb * 1e3 / steps / fwd_ms, 3),
+                "device_gb_used_peak": round(gb, 2)})
+    rel = lambda a, b: float(np.linalg.norm(a[act] - b[act]) / np.linalg.norm(b[act]))
+    col = lambda g: [float(g[y, x]) for x, y in cols]
+    _, ga64, tf64, tb64, _ = run_adjoint(args.precision, c, a64=True)
+    out["fp64_adjoint_same_trajectory"] = {"backward_s": round(tb64, 1), "lid": col(ga64)}
+    out["i_adjoint_rounding"] = {"field_rel_l2": rel(g32, ga64),
+                                 "columns_rel": [abs(a - b) / abs(b) for a, b in zip(col(g32), col(ga64))]}
+
+    # central differences of the 16-bit model, h halving, Richardson
+    hs = [float(h) for h in args.fd16_h.split(",")]
+    fd16 = []
+    for (x, y) in cols:
+        vals = []
+        for h in hs:
+            lp, lm = lid.copy(), lid.copy()
+            lp[x + y * dim] += h
+            lm[x + y * dim] -= h
+            vals.append((_loss(dim, steps, lp, tau, plane, target, args.precision, stride=0) -
+                         _loss(dim, steps, lm, tau, plane, target, args.precision, stride=0)) / (2 * h))
+        rich = [(4 * vals[k + 1] - vals[k]) / 3 for k in range(len(vals) - 1)]
+        fd16.append({"x": x, "y": y, "fd": vals, "richardson": rich})
+    best16 = [r["richardson"][-1] for r in fd16]
+    # the spread of the extrapolations is the FD's own uncertainty
+    unc16 = [abs(r["richardson"][-1] - r["richardson"][-2]) / abs(r["richardson"][-1]) if len(r["richardson"]) > 1
+             else None for r in fd16]
+    out["fd_16bit_model"] = {"h": hs, "columns": fd16}
+    out["ii_storage_linearisation"] = {
+        "columns_rel": [abs(a - b) / abs(b) for a, b in zip(col(ga64), best16)],
+        "fd_uncertainty_rel": unc16}
+
+    if args.fp64_adjoint:
+        c64 = args.fp64_every
+        J64, g64, tf, tb, gb = run_adjoint("fp64", c64)
+        out["fp64_model"] = {"loss": J64, "checkpoint_every": c64, "forward_s": round(tf, 1),
+                             "backward_s": round(tb, 1), "device_gb_used": round(gb, 1), "lid": col(g64)}
+        out["iii_model_difference"] = {"field_rel_l2": rel(ga64, g64),
+                                       "columns_rel": [abs(a - b) / abs(b) for a, b in zip(col(ga64), col(g64))]}
+        out["total_fp32_adjoint_vs_fp64_model"] = {
+            "field_rel_l2": rel(g32, g64),
+            "columns_rel": [abs(a - b) / abs(b) for a, b in zip(col(g32), col(g64))]}
+        h = 1e-6
+        rows = []
+        for (x, y) in cols[:args.fd64_columns]:
+            lp, lm = lid.copy(), lid.copy()
+            lp[x + y * dim] += h
+            lm[x + y * dim] -= h
+            d = (_loss(dim, steps, lp, tau, plane, target, "fp64", stride=0) -
+                 _loss(dim, steps, lm, tau, plane, target, "fp64", stride=0)) / (2 * h)
+            rows.append({"x": x, "y": y, "fd_fp64": d, "adjoint_fp64": float(g64[y, x]),
+                         "rel_fp64": abs(g64[y, x] - d) / abs(d), "adjoint_fp32_16bit": float(g32[y, x]),
+                         "rel_fp32_16bit": abs(g32[y, x] - d) / abs(d)})
+        out["fp64_exactness_fd_h1e-6"] = rows
     print(json.dumps(out), flush=True)
 
 
@@ -276,6 +319,8 @@ def main(argv=None) -> int:
     p.add_argument("--precision", default="fp16")
     p.add_argument("--fp64-adjoint", action="store_true")
     p.add_argument("--fp64-every", type=int, default=500, help="top-level checkpoint interval of the FP64 adjoint")
+    p.add_argument("--fd16-h", default="1e-3,5e-4,2.5e-4", help="steps of the 16-bit model's central differences")
+    p.add_argument("--fd64-columns", type=int, default=4, help="columns checked by FP64 central differences")
     p.add_argument("--seed", type=int, default=1234)
     a = ap.parse_args(argv)
     {"storage": storage, "adjoint": adjoint, "lidfield": lidfield}[a.cmd](a)

@@ -128,33 +128,47 @@ float lbmo_logf(float x)
 
 double lbmo_log(double x) { return (double)lbmo_logf((float)x); }
 
-/* Uniform in (-1, 1) from a 32-bit word (24 random bits). */
-static inline float lbmo_sym_uniform(uint32_t a)
+/* Uniform in (-1, 1) from 16 random bits: (a + 1/2) / 2^15 - 1, exact in float. */
+static inline float lbmo_sym_uniform16(uint32_t a)
 {
-    const float u01 = ((float)(a >> 8) + 0.5f) * (1.0f / 16777216.0f);
-    return (2.0f * u01) - 1.0f;
+    return (((float)a + 0.5f) * (1.0f / 32768.0f)) - 1.0f;
 }
 
-/* Standard normal by the Marsaglia polar method on the counter stream
- * (site, q, attempt), single precision; each Philox block offers two
- * attempts; at most 64 attempts, so the loop always ends. */
-float lbmo_gaussf(uint64_t seed, uint64_t site, uint32_t q)
+/* Two standard normals for (seed, site, pair) by the Marsaglia polar method:
+ * Philox4x32-10 on the counter (site_lo, site_hi, pair, block); each 32-bit
+ * output word is one attempt (its low and high 16 bits give v1, v2), so a
+ * block offers four attempts; the first accepted attempt gives both
+ * v1 r and v2 r, r = sqrt(-2 ln s / s).  Single precision, IEEE + - * /
+ * sqrt only; at most 64 attempts, so the loop always ends. */
+void lbmo_gauss_pairf(uint64_t seed, uint64_t site, uint32_t pair, float z[2])
 {
     const uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
-    for (uint32_t block = 0; block < 32; ++block) {
-        const uint32_t ctr[4] = {(uint32_t)site, (uint32_t)(site >> 32), q, block};
+    for (uint32_t block = 0; block < 16; ++block) {
+        const uint32_t ctr[4] = {(uint32_t)site, (uint32_t)(site >> 32), pair, block};
         uint32_t r[4];
         lbmo_philox4x32_10(ctr, key, r);
-        for (int half = 0; half < 2; ++half) {
-            const float v1 = lbmo_sym_uniform(r[2 * half]);
-            const float v2 = lbmo_sym_uniform(r[2 * half + 1]);
+        for (int a = 0; a < 4; ++a) {
+            const float v1 = lbmo_sym_uniform16(r[a] & 0xffffu);
+            const float v2 = lbmo_sym_uniform16(r[a] >> 16);
             const float s = (v1 * v1) + (v2 * v2);
             if (s >= 1.0f || s == 0.0f) continue;
             const float t = (-2.0f * lbmo_logf(s)) / s;
-            return v1 * sqrtf(t);
+            const float rt = sqrtf(t);
+            z[0] = v1 * rt;
+            z[1] = v2 * rt;
+            return;
         }
     }
-    return 0.0f;
+    z[0] = 0.0f;
+    z[1] = 0.0f;
+}
+
+/* The sample of population q of a site: element q & 1 of pair q >> 1. */
+float lbmo_gaussf(uint64_t seed, uint64_t site, uint32_t q)
+{
+    float z[2];
+    lbmo_gauss_pairf(seed, site, q >> 1, z);
+    return z[q & 1u];
 }
 
 double lbmo_gauss(uint64_t seed, uint64_t site, uint32_t q) { return (double)lbmo_gaussf(seed, site, q); }

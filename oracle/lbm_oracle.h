@@ -61,9 +61,12 @@ typedef struct lbmo_params {
 int lbmo_cell_type(int dim, int x, int y, int z);
 
 /* Standard normal sample for (seed, site, q): Philox4x32-10 counter stream,
- * Marsaglia polar method, a self-contained natural logarithm.  Computed with
- * IEEE single-precision + - * / sqrt only, so the GPU library reproduces it
- * bit for bit.  lbmo_gauss returns the same value widened to double. */
+ * Marsaglia polar method (both normals of an accepted attempt: populations
+ * 2m and 2m+1 share pair m), a self-contained natural logarithm.  Computed
+ * with IEEE single-precision + - * / sqrt only, so the GPU library
+ * reproduces it bit for bit.  lbmo_gauss returns the same value widened to
+ * double; lbmo_gauss_pairf gives both samples of one pair. */
+void lbmo_gauss_pairf(uint64_t seed, uint64_t site, uint32_t pair, float z[2]);
 float lbmo_gaussf(uint64_t seed, uint64_t site, uint32_t q);
 double lbmo_gauss(uint64_t seed, uint64_t site, uint32_t q);
 

@@ -74,12 +74,16 @@ void SFX(lbmo_init)(const lbmo_params *p, REAL *f_stream, REAL *f_collide,
                 u[1 * n + id] = sm ? uy : qnan;
                 u[2 * n + id] = sm ? uz : qnan;
                 const REAL u2 = ((ux * ux) + (uy * uy)) + (uz * uz);
+                /* seeded perturbation of FLUID populations, both buffers:
+                 * populations 2m and 2m+1 take the two samples of pair m */
+                float z[LBMO_Q + 1];
+                const int noisy = p->noise_sigma != 0.0 && ct == LBMO_FLUID;
+                if (noisy)
+                    for (int m = 0; m < (LBMO_Q + 1) / 2; ++m) lbmo_gauss_pairf(p->seed, id, (uint32_t)m, z + 2 * m);
                 for (int i = 0; i < LBMO_Q; ++i) {
                     REAL fi = SFX(feq)(i, r0, ux, uy, uz, u2, w);
                     if (lbmo_is_wall(ct)) fi = qnan;
-                    /* seeded perturbation of FLUID populations, both buffers */
-                    if (p->noise_sigma != 0.0 && ct == LBMO_FLUID)
-                        fi = fi + (REAL)(p->noise_sigma * lbmo_gauss(p->seed, id, (uint32_t)i));
+                    if (noisy) fi = fi + (REAL)(p->noise_sigma * (double)z[i]);
                     f_collide[SFX(csoa)(id, i, sd)] = fi;
                     f_stream[SFX(csoa)(id, i, sd)] = fi;
                 }
