@@ -123,7 +123,11 @@ typedef enum lbm_kernel {
     LBM_KERNEL_DIRECT = 1,   /* per-thread 16-byte vector loads straight from HBM        */
     LBM_KERNEL_STAGED = 2,   /* persistent CTAs; whole source rows staged in shared
                                 memory by cp.async.bulk (TMA) through an mbarrier ring   */
-    LBM_KERNEL_NARROW = 3    /* as DIRECT with 8-byte vectors (fewer registers)          */
+    LBM_KERNEL_NARROW = 3,   /* as DIRECT with 8-byte vectors (fewer registers)          */
+    LBM_KERNEL_AA = 4        /* one lattice updated in place, alternating a local step and
+                                a neighbour step (AA pattern): half the population memory;
+                                LBM_DUMP_F_RAW then holds the current step's layout, and
+                                the lbm_adjoint_* calls are not available                 */
 } lbm_kernel;
 
 /* Fill *c with the reference CLI defaults (lbm_options.hpp:83-101):

@@ -137,10 +137,19 @@ bool two_step(const lbm_t *h)
     return adj2_grid(h, ntx, nty) >= 2u * (unsigned)std::max(h->num_sms, 1);
 }
 
+// the stored-point sweep's two-step kernel: with the next plane's loads
+// prefetched (1, default) or without (0)
+#ifndef LBM_ADJ2_PREFETCH
+#define LBM_ADJ2_PREFETCH 1
+#endif
+
 template <class S, bool MACRO>
 cudaError_t run_adjoint2(const lbm::Adj2Args &a, unsigned grid, cudaStream_t s)
 {
-    lbm::adjoint2_kernel<S, MACRO><<<grid, lbm::ADJ2_EX * lbm::ADJ2_EY, lbm::ADJ2_SMEM, s>>>(a);
+    if (MACRO && LBM_ADJ2_PREFETCH)
+        lbm::adjoint2p_kernel<S><<<grid, lbm::ADJ2_EX * lbm::ADJ2_EY, lbm::ADJ2_SMEM, s>>>(a);
+    else
+        lbm::adjoint2_kernel<S, MACRO><<<grid, lbm::ADJ2_EX * lbm::ADJ2_EY, lbm::ADJ2_SMEM, s>>>(a);
     return cudaGetLastError();
 }
 
@@ -151,6 +160,7 @@ cudaError_t set_adjoint2_smem()
     const cudaFuncAttribute at = cudaFuncAttributeMaxDynamicSharedMemorySize;
     cudaError_t e = cudaFuncSetAttribute(lbm::adjoint2_kernel<S, false>, at, bytes);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(lbm::adjoint2_kernel<S, true>, at, bytes);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(lbm::adjoint2p_kernel<S>, at, bytes);
     return e;
 }
 
@@ -508,6 +518,9 @@ int lbm_adjoint_forward(lbm_t *h, int iterations, int checkpoint_every, double *
     if (iterations < 1 || checkpoint_every < 1)
         return fail(LBM_EINVAL, "lbm_adjoint_forward: iterations and checkpoint_every must be >= 1");
     if (h->adj.plane_y < 0) return fail(LBM_ESTATE, "lbm_adjoint_forward: call lbm_adjoint_set_loss first");
+    if (h->kernel == LBM_KERNEL_AA)
+        return fail(LBM_ESTATE, "lbm_adjoint_forward: the adjoint needs the two-lattice kernels "
+                                "(LBM_KERNEL_AA keeps one lattice in place)");
     lbm_adjoint_state &s = h->adj;
     const size_t fbytes = (size_t)lbm::Q * h->n * lbm::storage_bytes(h->prec);
     // drop the previous run's state buffers (the target and work buffers

@@ -148,11 +148,16 @@ void release(lbm_t *h)
     delete h;
 }
 
-lbm::StepArgs step_args(const lbm_t *h, int from)
+bool is_aa(const lbm_t *h) { return h->kernel == LBM_KERNEL_AA; }
+
+// Iteration arguments from buffer `from` (two-lattice kernels) or of AA
+// phase `phase` (the one lattice f[0]).
+lbm::StepArgs step_args(const lbm_t *h, int from, int phase)
 {
     lbm::StepArgs a;
-    a.fin = h->f[from];
-    a.fout = h->f[from ^ 1];
+    a.fin = is_aa(h) ? h->f[0] : h->f[from];
+    a.fout = is_aa(h) ? h->f[0] : h->f[from ^ 1];
+    a.aa_phase = phase;
     a.map = h->map;
     a.lid = h->lid;
     a.rho = h->rho;
@@ -170,6 +175,21 @@ lbm::StepArgs step_args(const lbm_t *h, int from)
     a.ngroups = h->ngroups;
     a.stages = h->stages;
     return a;
+}
+lbm::StepArgs step_args(const lbm_t *h, int from) { return step_args(h, from, h->aa_phase); }
+
+// the buffer parity (two lattices) or phase (AA) of the current state, and
+// its flip after one iteration
+int parity(const lbm_t *h) { return is_aa(h) ? h->aa_phase : h->cur; }
+void flip(lbm_t *h)
+{
+    if (is_aa(h)) h->aa_phase ^= 1;
+    else h->cur ^= 1;
+}
+// layout of the current state for the dump / load kernels
+int state_layout(const lbm_t *h)
+{
+    return is_aa(h) ? (h->aa_phase ? lbm::LAYOUT_AA_B : lbm::LAYOUT_AA_A) : lbm::LAYOUT_PULL;
 }
 
 const void *staged_ptr(int prec, int mode)
@@ -223,6 +243,14 @@ int setup_staged(lbm_t *h, int want_stages)
 
 cudaError_t launch_pull(const lbm_t *h, int mode, const lbm::StepArgs &a, unsigned *nparts = nullptr)
 {
+    if (h->kernel == LBM_KERNEL_AA) {
+        switch (h->prec) {
+        case LBM_FP32: return lbm::launch_aa_f32(mode, a, h->block, h->stream, nparts);
+        case LBM_FP64: return lbm::launch_aa_f64(mode, a, h->block, h->stream, nparts);
+        case LBM_FP16: return lbm::launch_aa_f16(mode, a, h->block, h->stream, nparts);
+        default: return lbm::launch_aa_bf16(mode, a, h->block, h->stream, nparts);
+        }
+    }
     if (h->kernel == LBM_KERNEL_STAGED && (mode == lbm::MODE_STEP || mode == lbm::MODE_STEP_MACRO)) {
         switch (h->prec) {
         case LBM_FP32: return lbm::launch_staged_f32(mode, a, h->sgrid, h->sblock, h->ssmem, h->stream);
@@ -262,14 +290,15 @@ bool macro_within(int64_t it0, int G, int macro_every)
 // call.
 cudaError_t replay_graph(lbm_t *h)
 {
-    cudaGraphExec_t &exec = h->graph_exec[h->cur];
+    cudaGraphExec_t &exec = h->graph_exec[parity(h)];
     if (!exec) {
         cudaError_t e = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal);
         if (e != cudaSuccess) return e;
-        int cur = h->cur;
+        int cur = h->cur, ph = h->aa_phase;
         for (int k = 0; k < h->graph_iters && e == cudaSuccess; ++k) {
-            e = launch_pull(h, lbm::MODE_STEP, step_args(h, cur));
-            cur ^= 1;
+            e = launch_pull(h, lbm::MODE_STEP, step_args(h, cur, ph));
+            if (is_aa(h)) ph ^= 1;
+            else cur ^= 1;
         }
         cudaGraph_t g = nullptr;
         const cudaError_t ec = cudaStreamEndCapture(h->stream, &g);
@@ -366,7 +395,7 @@ int lbm_init(lbm_t **out, const lbm_config *c)
     if (!std::isfinite(c->velocity)) return fail(LBM_EINVAL, "lbm_init: velocity must be finite");
     if (c->noise_sigma < 0.0 || !std::isfinite(c->noise_sigma))
         return fail(LBM_EINVAL, "lbm_init: noise_sigma must be finite and >= 0");
-    if (c->kernel < LBM_KERNEL_AUTO || c->kernel > LBM_KERNEL_NARROW)
+    if (c->kernel < LBM_KERNEL_AUTO || c->kernel > LBM_KERNEL_AA)
         return fail(LBM_EINVAL, "lbm_init: unknown kernel variant %d", c->kernel);
     if (c->stages < 0 || c->stages > 16) return fail(LBM_EINVAL, "lbm_init: stages %d out of range", c->stages);
     if (c->adjoint_steps < 0 || c->adjoint_steps > 2)
@@ -392,13 +421,17 @@ int lbm_init(lbm_t **out, const lbm_config *c)
     unsigned block = c->block_threads > 0 ? (unsigned)(c->block_threads / 32 * 32) : 128u;
     if (block < 32) block = 32;
     if (block > 256) block = 256;  // the pull kernel's launch bound
-    const size_t grid = (nvec + block - 1) / block;
+    // reduction partials: one pair per block of the widest launch (the AA
+    // variant's FP32 kernels use 8-byte vectors, twice the threads)
+    const int Vr = (c->kernel == LBM_KERNEL_AA && prec == LBM_FP32) ? V / 2 : V;
+    const size_t grid = ((size_t)(dim / Vr) * (size_t)(dim - 2) * (size_t)(dim - 2) + block - 1) / block;
     if (2 * nvec >= ((size_t)1 << 32)) return fail(LBM_EINVAL, "lbm_init: lattice too large");
 
     const size_t sb = storage_bytes(prec), mb = macro_bytes(prec);
     const size_t fbytes = (size_t)lbm::Q * n * sb;
     const size_t stage_elems = std::min(kStageElems, (size_t)lbm::Q * n);
-    const size_t need = 2 * fbytes + n + 4 * n * mb + (size_t)dim * dim * mb + stage_elems * dump_elem(prec) +
+    const bool aa = c->kernel == LBM_KERNEL_AA;  // one lattice
+    const size_t need = (aa ? 1 : 2) * fbytes + n + 4 * n * mb + (size_t)dim * dim * mb + stage_elems * dump_elem(prec) +
                         (grid + 2) * 2 * sizeof(double) + 4 * sizeof(double) + sizeof(int);
     if (c->max_device_bytes > 0 && need > c->max_device_bytes)
         return fail(LBM_ENOMEM, "lbm_init: needs %zu device bytes, budget is %zu", need, c->max_device_bytes);
@@ -441,7 +474,7 @@ int lbm_init(lbm_t **out, const lbm_config *c)
         LBM_CUDA(cudaEventCreate(&h->ev_first));
         LBM_CUDA(cudaEventCreate(&h->ev_last));
         LBM_CUDA(cudaMalloc(&h->f[0], fbytes));
-        LBM_CUDA(cudaMalloc(&h->f[1], fbytes));
+        if (!aa) LBM_CUDA(cudaMalloc(&h->f[1], fbytes));
         LBM_CUDA(cudaMalloc((void **)&h->map, n));
         LBM_CUDA(cudaMalloc(&h->rho, n * mb));
         LBM_CUDA(cudaMalloc(&h->u, 3 * n * mb));
@@ -472,6 +505,7 @@ int lbm_init(lbm_t **out, const lbm_config *c)
         ia.n = n;
         ia.seed = c->seed;
         ia.noise_sigma = c->noise_sigma;
+        ia.in_place = aa ? 1 : 0;
         LBM_CUDA(cudaEventRecord(h->ev_first, h->stream));
         switch (prec) {
         case LBM_FP32: LBM_CUDA(lbm::launch_init_f32(ia, h->stream)); break;
@@ -487,7 +521,7 @@ int lbm_init(lbm_t **out, const lbm_config *c)
         // 16-byte vectors for 16-bit storage and FP64, 8-byte vectors for FP32
         int want = c->kernel;
         if (want == LBM_KERNEL_AUTO) want = prec == LBM_FP32 ? LBM_KERNEL_NARROW : LBM_KERNEL_DIRECT;
-        h->kernel = LBM_KERNEL_DIRECT;
+        h->kernel = aa ? LBM_KERNEL_AA : LBM_KERNEL_DIRECT;
         if (want == LBM_KERNEL_NARROW && prec != LBM_FP64) {
             h->kernel = LBM_KERNEL_NARROW;
         }
@@ -533,7 +567,7 @@ int lbm_step(lbm_t *h, int nsteps, int macro_every)
         if (!per_step && G > 1 && nsteps - k >= G && !macro_within(h->it, G, macro_every)) {
             LBM_CUDA(replay_graph(h));
             k += G;
-            h->it += G;  // G is even: h->cur is unchanged
+            h->it += G;  // G is even: h->cur / h->aa_phase is unchanged
             continue;
         }
         ++k;
@@ -551,7 +585,7 @@ int lbm_step(lbm_t *h, int nsteps, int macro_every)
             LBM_CUDA(cudaEventRecord(s1, h->stream));
             h->pending.emplace_back(s0, s1);
         }
-        h->cur ^= 1;
+        flip(h);
         h->it = it;
     }
     if (!per_step) {
@@ -596,6 +630,7 @@ int lbm_dump(lbm_t *h, int what, void *dst, size_t bytes)
             a.dim = h->dim;
             a.sd = h->sd;
             a.n = h->n;
+            a.layout = state_layout(h);
             switch (h->prec) {
             case LBM_FP32: LBM_CUDA(lbm::launch_dump_f32(a, h->stream)); break;
             case LBM_FP64: LBM_CUDA(lbm::launch_dump_f64(a, h->stream)); break;
@@ -659,6 +694,7 @@ int lbm_load(lbm_t *h, int what, const void *src, size_t bytes)
             a.dim = h->dim;
             a.sd = h->sd;
             a.n = h->n;
+            a.layout = state_layout(h);
             LBM_CUDA(cudaMemcpyAsync(h->stage, (const char *)src + o0 * te, a.count * te, cudaMemcpyHostToDevice,
                                      h->stream));
             switch (h->prec) {

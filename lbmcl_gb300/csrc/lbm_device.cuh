@@ -317,6 +317,8 @@ struct StepArgs {
     int gpp;             // groups per z-plane = ceil((dim-2) / rows)
     unsigned ngroups;    // gpp * (dim-2)
     int stages;          // ring depth
+    // AA variant: fin == fout is the one lattice; 0 = A-step, 1 = B-step
+    int aa_phase;
 };
 
 // Initial-state kernel arguments.
@@ -329,17 +331,22 @@ struct InitArgs {
     size_t n;
     uint64_t seed;
     double noise_sigma;
+    int in_place;         // 1: the AA kernels' one lattice in A-form (f(s, i) = R_0(s, i));
+                          // 0: P_{-1} of the two-lattice kernels
 };
 
 // F dump / load kernel arguments (output element range [o0, o0 + count)).
 struct DumpArgs {
-    void *f;              // P (the current buffer)
+    void *f;              // the current buffer
     const uint8_t *map;
     const void *lid;
     void *buf;            // staging, T elements
     size_t o0, count;     // output range [o0, o0 + count)
     int dim, sd;          // sd = log2(stride), -1 for SoA of a non-power-of-two lattice
     size_t n;
+    int layout;           // LAYOUT_PULL: P of the two-lattice kernels; LAYOUT_AA_A / _B: the
+                          // AA lattice in A-form / B-form
 };
+enum { LAYOUT_PULL = -1, LAYOUT_AA_A = 0, LAYOUT_AA_B = 1 };
 
 }  // namespace lbm

@@ -51,7 +51,9 @@ struct lbm_handle {
     double inv_tau = 0;     // 1/tau rounded to the compute precision
     float omega_f = 0;
     void *f[2] = {nullptr, nullptr};
-    int cur = 0;            // f[cur] holds P_{t-1}
+    int cur = 0;            // f[cur] holds P_{t-1} (always 0 for the AA variant)
+    int aa_phase = 0;       // AA variant (one lattice): 0 = A-form, next an A-step;
+                            // 1 = B-form, next a B-step
     uint8_t *map = nullptr;
     void *rho = nullptr;
     void *u = nullptr;

@@ -671,8 +671,14 @@ template <class S, int VB> constexpr int min_blocks()
                           : LBM_MINB_64;
 }
 
+// largest block the pull / AA kernels are compiled for (the launcher clamps
+// block_threads to it)
+#ifndef LBM_PULL_MAXT
+#define LBM_PULL_MAXT 256
+#endif
+
 template <class S, int MODE, int VB, int ROWS>
-__global__ void __launch_bounds__(256, min_blocks<S, VB>()) pull_kernel(StepArgs a)
+__global__ void __launch_bounds__(LBM_PULL_MAXT, min_blocks<S, VB>()) pull_kernel(StepArgs a)
 {
     constexpr int V = VB / (int)sizeof(S);
     const unsigned g = blockIdx.x * blockDim.x + threadIdx.x;
@@ -692,6 +698,188 @@ __global__ void __launch_bounds__(256, min_blocks<S, VB>()) pull_kernel(StepArgs
         }
         pull_vector<S, MODE, V, ROWS == ROWS_INTERIOR>(a, xv, y, z, red_m, red_e);
     }
+    if (MODE == MODE_REDUCE) block_reduce_write(red_m, red_e, a.partials + 2 * (size_t)a.partial_base);
+}
+
+// ---------------------------------------------------------------------------
+// AA pattern: one lattice updated in place, two kinds of iteration.
+//   A-form buffer: f(s, i) = R(s, i), the post-stream value of slot (s, i)
+//   B-form buffer: f(s, opp i) = P_i(s), the post-collision value of site s
+// A-step (A-form -> B-form): every site reads its own 19 slots and writes its
+// post-collision populations to its own opposite slots; aligned vectors, no
+// neighbour.  B-step (B-form -> A-form): site s reads g_i = f(s - e_i, opp i)
+// (the pull of the two-lattice kernel, from the opposite population) and
+// writes P_i(s) to f(s + e_i, i).  Each slot is read and written by one site
+// per step, reads first, so the update is race-free in place.  The B-step's
+// x-shifted stores are realigned in registers: a lane's aligned destination
+// vector takes one element from its neighbour lane (warp shuffle); the
+// element that crosses a warp boundary is stored by its own lane as a
+// scalar, and the receiving lane stores the rest of its vector element-wise.
+// Lanes of wall sites compute garbage that lands only in wall slots whose
+// source is a wall (or outside the lattice) and in wall-sourced slots of
+// boundary sites: slots that no iteration and no dump reads.
+// ---------------------------------------------------------------------------
+template <class S> __device__ __forceinline__ S shfl_elem(S v, int delta, bool up)
+{
+    if constexpr (sizeof(S) == 2) {
+        unsigned short u;
+        memcpy(&u, &v, 2);
+        const int r = up ? __shfl_up_sync(0xffffffffu, (int)u, delta) : __shfl_down_sync(0xffffffffu, (int)u, delta);
+        const unsigned short ur = (unsigned short)r;
+        S o;
+        memcpy(&o, &ur, 2);
+        return o;
+    } else {
+        return up ? __shfl_up_sync(0xffffffffu, v, delta) : __shfl_down_sync(0xffffffffu, v, delta);
+    }
+}
+
+// out[k] (site x0 + k) to position x0 + k + EX of a row (`row` at x = 0).
+// Every lane of the warp calls this (the shuffles); inactive lanes store
+// nothing.
+template <class S, int V, int EX>
+__device__ __forceinline__ void store_row_shifted(S *__restrict__ row, int x0, int dim, const S (&out)[V],
+                                                  bool active, int lane)
+{
+    if constexpr (EX == 0) {
+        if (active) store_vec<S, V>(row + x0, out);
+    } else if constexpr (EX == 1) {
+        const S prev = shfl_elem(out[V - 1], 1, true);
+        if (!active) return;
+        S v[V];
+        v[0] = prev;
+#pragma unroll
+        for (int k = 1; k < V; ++k) v[k] = out[k - 1];
+        if (lane != 0 || x0 == 0) {
+            store_vec<S, V>(row + x0, v);  // at a row start v[0] is a wall slot's don't-care
+        } else {
+#pragma unroll
+            for (int k = 1; k < V; ++k) row[x0 + k] = v[k];
+        }
+        if (lane == 31 && x0 + V < dim) row[x0 + V] = out[V - 1];
+    } else {
+        const S next = shfl_elem(out[0], 1, false);
+        if (!active) return;
+        S v[V];
+#pragma unroll
+        for (int k = 0; k < V - 1; ++k) v[k] = out[k + 1];
+        v[V - 1] = next;
+        if (lane != 31 || x0 + V == dim) {
+            store_vec<S, V>(row + x0, v);  // at a row end v[V-1] is a wall slot's don't-care
+        } else {
+#pragma unroll
+            for (int k = 0; k < V - 1; ++k) row[x0 + k] = v[k];
+        }
+        if (lane == 0 && x0 > 0) row[x0 - 1] = out[0];
+    }
+}
+
+// The pre-collision populations of V sites from the one lattice.
+template <class S, int V, int I, int PHASE>
+__device__ __forceinline__ void gather_aa(const S *__restrict__ f, size_t n, size_t rowoff, int dim, int x0,
+                                          S (&fs)[Q][V])
+{
+    if constexpr (PHASE == 0) {
+        load_vec<S, V>(f + (size_t)I * n + rowoff + x0, fs[I]);
+    } else {
+        const ptrdiff_t shift = (ptrdiff_t)ez_of(I) * dim * dim + (ptrdiff_t)ey_of(I) * dim;
+        gather_row<S, V, ex_of(I)>(f + (size_t)opp_of(I) * n + rowoff - shift, x0, dim, fs[I]);
+    }
+    if constexpr (I + 1 < Q) gather_aa<S, V, I + 1, PHASE>(f, n, rowoff, dim, x0, fs);
+}
+
+// Bounce-back of the x-face site xf of an interior row (see face_fix): its
+// output i is its input opp(i), a wall-sourced input being the constant.
+template <class S, int V, int PHASE>
+__device__ __forceinline__ void face_fix_aa(const StepArgs &a, size_t rowoff, int xf, int k, S (&fs)[Q][V])
+{
+    using C = typename Compute<S>::type;
+    const S *__restrict__ f = static_cast<const S *>(a.fout);
+    const int dim = a.dim;
+    const Weights<C> W = make_weights<C>();
+#pragma unroll
+    for (int i = 0; i < Q; ++i) {
+        const int j = opp_of(i);
+        const int sx = xf - ex_of(j);
+        S v;
+        if (sx == 0 || sx == dim - 1) {
+            if constexpr (is_dev16<S>()) v = zero_elem<S>();
+            else v = (S)W.w[wclass_of(j)];
+        } else if constexpr (PHASE == 0) {
+            v = load_one(f + (size_t)j * a.n + rowoff + xf);  // own slot j
+        } else {
+            const ptrdiff_t shift = (ptrdiff_t)ez_of(j) * dim * dim + (ptrdiff_t)ey_of(j) * dim;
+            v = load_one(f + (size_t)i * a.n + rowoff - shift + sx);  // f(s - e_j, opp j)
+        }
+        fs[i][k] = v;
+    }
+}
+
+template <class S, int MODE, int V, bool INTERIOR, int PHASE>
+__device__ __forceinline__ void aa_vector(const StepArgs &a, bool active, int xv, int y, int z, double &red_m,
+                                          double &red_e)
+{
+    const int dim = a.dim;
+    const int x0 = xv * V;
+    const size_t rowoff = (size_t)z * dim * dim + (size_t)y * dim;
+    const size_t site0 = rowoff + (size_t)x0;
+    S *__restrict__ f = static_cast<S *>(a.fout);
+    S fs[Q][V];
+    if (active) {
+        typename MapWord<V>::type mw = 0;
+        if (!INTERIOR) mw = __ldg(reinterpret_cast<const typename MapWord<V>::type *>(a.map + site0));
+        gather_aa<S, V, 0, PHASE>(f, a.n, rowoff, dim, x0, fs);
+        update_vector<S, MODE, V, INTERIOR>(fs, mw, a, y, z, x0, site0, red_m, red_e);
+        if (INTERIOR && MODE != MODE_REDUCE) {
+            if (x0 == 0) face_fix_aa<S, V, PHASE>(a, rowoff, 1, 1, fs);
+            if (x0 + V == dim) face_fix_aa<S, V, PHASE>(a, rowoff, dim - 2, V - 2, fs);
+        }
+    }
+    if constexpr (MODE != MODE_REDUCE) {
+        if constexpr (PHASE == 0) {
+            if (active) {
+#pragma unroll
+                for (int i = 0; i < Q; ++i) store_vec<S, V>(f + (size_t)opp_of(i) * a.n + site0, fs[i]);
+            }
+        } else {
+            const int lane = (int)(threadIdx.x & 31);
+#pragma unroll
+            for (int i = 0; i < Q; ++i) {
+                const ptrdiff_t shift = (ptrdiff_t)ez_of(i) * dim * dim + (ptrdiff_t)ey_of(i) * dim;
+                S *row = f + (size_t)i * a.n + (size_t)((ptrdiff_t)rowoff + shift);
+                if (ex_of(i) == 1) store_row_shifted<S, V, 1>(row, x0, dim, fs[i], active, lane);
+                else if (ex_of(i) == -1) store_row_shifted<S, V, -1>(row, x0, dim, fs[i], active, lane);
+                else store_row_shifted<S, V, 0>(row, x0, dim, fs[i], active, lane);
+            }
+        }
+    }
+}
+
+// One AA iteration (or reduction pass) over the rows of one kind; a.fout is
+// the lattice, PHASE 0 = A-step, 1 = B-step.  Same row split and register
+// caps as pull_kernel.
+template <class S, int MODE, int VB, int ROWS, int PHASE>
+__global__ void __launch_bounds__(256, min_blocks<S, VB>()) aa_kernel(StepArgs a)
+{
+    constexpr int V = VB / (int)sizeof(S);
+    const unsigned g = blockIdx.x * blockDim.x + threadIdx.x;
+    double red_m = 0.0, red_e = 0.0;
+    const unsigned nrows = ROWS == ROWS_INTERIOR ? (unsigned)(a.dim - 4) * (unsigned)(a.dim - 4)
+                                                 : 4u * (unsigned)(a.dim - 3);
+    const bool active = g < nrows * (unsigned)a.nvx;
+    int y = 2, z = 2, xv = 0;
+    if (active) {
+        const int dim = a.dim;
+        const unsigned row = g / (unsigned)a.nvx;
+        xv = (int)(g - row * (unsigned)a.nvx);
+        if (ROWS == ROWS_INTERIOR) {
+            y = 2 + (int)(row % (unsigned)(dim - 4));
+            z = 2 + (int)(row / (unsigned)(dim - 4));
+        } else {
+            decode_face_row(dim, row, y, z);
+        }
+    }
+    aa_vector<S, MODE, V, ROWS == ROWS_INTERIOR, PHASE>(a, active, xv, y, z, red_m, red_e);
     if (MODE == MODE_REDUCE) block_reduce_write(red_m, red_e, a.partials + 2 * (size_t)a.partial_base);
 }
 
@@ -946,7 +1134,23 @@ __global__ void init_kernel(InitArgs a)
 #pragma unroll
     for (int i = 0; i < Q; ++i) {
         C val = qn;  // walls hold NaN (kernels.cl:312, 316)
-        if (!(b & M_WALL)) {
+        if (a.in_place) {
+            // A-form: the site's own R_0 slots, its initial equilibrium (the
+            // noise of FLUID sites is written by noise_kernel)
+            if (!(b & M_WALL)) {
+                const C lv = (b & M_FRONT) ? lid_at<C>(a, x, y) : (C)0;
+                if constexpr (is_dev16<S>()) {
+                    float d = 0.0f;
+                    if (b & M_FRONT) {
+                        const float eu = ex_of(i) > 0 ? (float)lv : (ex_of(i) < 0 ? -(float)lv : 0.0f);
+                        d = deq_scaled(i, 0.0f, 1.0f, eu, 1.5f * (float)lv * (float)lv, 1.0f);
+                    }
+                    val = d * Dev16<S>::scale;
+                } else {
+                    val = (b & M_FRONT) ? init_eq_exact<C>(i, lv, W) : W.w[wclass_of(i)];
+                }
+            }
+        } else if (!(b & M_WALL)) {
             const int tx = x + ex_of(i), ty = y + ey_of(i), tz = z + ez_of(i);
             const uint8_t tb = pack_cell(dim, tx, ty, tz);
             if (!(tb & M_WALL)) {
@@ -976,8 +1180,9 @@ __global__ void init_kernel(InitArgs a)
 // Seeded N(0, sigma^2) noise on the initial populations of the FLUID sites
 // (x, y, z in [2, dim-3]), run after init_kernel: the thread of FLUID site t
 // draws its ten sample pairs (populations 2m, 2m+1 <- pair m) and writes the
-// 19 slots (t - e_q, q) of P_{-1} that stream into t, each slot having this
-// one writer: the equilibrium at rest (w_q; deviation 0) plus sigma z.
+// 19 slots (t - e_q, q) of P_{-1} that stream into t (in place: t's own
+// slots (t, q)), each slot having this one writer: the equilibrium at rest
+// (w_q; deviation 0) plus sigma z.
 template <class S>
 __global__ void noise_kernel(InitArgs a)
 {
@@ -999,7 +1204,8 @@ __global__ void noise_kernel(InitArgs a)
             const int q = 2 * p + h;
             if (q >= Q) break;
             const double sz = __dmul_rn(a.noise_sigma, (double)(h ? z1 : z0));
-            const ptrdiff_t sh = (ptrdiff_t)ex_of(q) + (ptrdiff_t)ey_of(q) * dim + (ptrdiff_t)ez_of(q) * dim * dim;
+            const ptrdiff_t sh = a.in_place ? 0
+                               : (ptrdiff_t)ex_of(q) + (ptrdiff_t)ey_of(q) * dim + (ptrdiff_t)ez_of(q) * dim * dim;
             S *dst = f + (size_t)q * a.n + (size_t)((ptrdiff_t)t - sh);
             if constexpr (is_dev16<S>()) {
                 const float val = __fmul_rn((float)sz, Dev16<S>::scale);
@@ -1031,16 +1237,18 @@ __device__ __forceinline__ void decode_csoa(size_t o, int sd, size_t n, size_t &
     id = ((t / Q) << sd) | lane;
 }
 
+// the value of population q held in slot (at, qs)
 template <class S, class C>
-__device__ __forceinline__ C stored_value(const S *f, size_t n, int q, size_t src)
+__device__ __forceinline__ C stored_value(const S *f, size_t n, int qs, size_t at, int q)
 {
-    const S v = f[(size_t)q * n + src];
+    const S v = f[(size_t)qs * n + at];
     if constexpr (is_dev16<S>()) {
         return (C)(wf_of(q) + Dev16<S>::to_f(v) * Dev16<S>::inv_scale);
     } else {
         return (C)v;
     }
 }
+
 
 template <class S, class T>
 __global__ void dump_f_kernel(DumpArgs a)
@@ -1059,15 +1267,19 @@ __global__ void dump_f_kernel(DumpArgs a)
     const size_t src = in ? (size_t)sx + (size_t)sy * dim + (size_t)sz * dim * dim : 0;
     const bool src_wall = !in || (a.map[src] & M_WALL);
     const S *f = static_cast<const S *>(a.f);
+    // where R(id, q) lives: P(src, q) (two-lattice), f(id, q) (AA A-form),
+    // f(src, opp q) (AA B-form)
+    const int qs = a.layout == LAYOUT_AA_B ? opp_of(q) : q;
+    const size_t at = a.layout == LAYOUT_AA_A ? id : src;
     T val;
     if (b & M_WALL) {
-        val = src_wall ? (T)nan_of<C>() : (T)stored_value<S, C>(f, a.n, q, src);
+        val = src_wall ? (T)nan_of<C>() : (T)stored_value<S, C>(f, a.n, qs, at, q);
     } else if (src_wall) {
         const Weights<C> W = make_weights<C>();
         C lv = (b & M_FRONT) ? static_cast<const C *>(a.lid)[(size_t)y * dim + x] : (C)0;
         val = (T)((b & M_FRONT) ? init_eq_exact<C>(q, lv, W) : W.w[wclass_of(q)]);
     } else {
-        val = (T)stored_value<S, C>(f, a.n, q, src);
+        val = (T)stored_value<S, C>(f, a.n, qs, at, q);
     }
     static_cast<T *>(a.buf)[k] = val;
 }
@@ -1088,10 +1300,11 @@ __global__ void load_f_kernel(DumpArgs a)
     if (a.map[src] & M_WALL) return;
     const T v = static_cast<const T *>(a.buf)[k];
     S *f = static_cast<S *>(a.f);
+    const size_t slot = (size_t)(a.layout == LAYOUT_AA_B ? opp_of(q) : q) * a.n + (a.layout == LAYOUT_AA_A ? id : src);
     if constexpr (is_dev16<S>()) {
-        f[(size_t)q * a.n + src] = Dev16<S>::from_f(((float)v - wf_of(q)) * Dev16<S>::scale);
+        f[slot] = Dev16<S>::from_f(((float)v - wf_of(q)) * Dev16<S>::scale);
     } else {
-        f[(size_t)q * a.n + src] = (S)v;
+        f[slot] = (S)v;
     }
 }
 

@@ -51,6 +51,57 @@ static cudaError_t launch_direct(int mode, const StepArgs &a0, unsigned block, c
     return cudaSuccess;
 }
 
+// One AA iteration (or reduction pass) of phase PHASE: interior rows, then
+// face rows, as launch_direct.
+template <int VB, int PHASE>
+static cudaError_t launch_aa_phase(int mode, const StepArgs &a0, unsigned block, cudaStream_t s, unsigned *nparts)
+{
+    constexpr int V = VB / (int)sizeof(LBM_S);
+    StepArgs a = a0;
+    a.nvx = a0.dim / V;
+    const size_t m = (size_t)(a.dim - 4);
+    const unsigned gi = (unsigned)((m * m * (size_t)a.nvx + block - 1) / block);
+    const unsigned gf = (unsigned)(((size_t)4 * (a.dim - 3) * (size_t)a.nvx + block - 1) / block);
+    for (int pass = 0; pass < 2; ++pass) {
+        const unsigned grid = pass == 0 ? gi : gf;
+        if (grid == 0) continue;
+        a.partial_base = pass == 0 ? 0u : gi;
+        if (pass == 0) {
+            switch (mode) {
+            case MODE_STEP: aa_kernel<LBM_S, MODE_STEP, VB, ROWS_INTERIOR, PHASE><<<grid, block, 0, s>>>(a); break;
+            case MODE_STEP_MACRO:
+                aa_kernel<LBM_S, MODE_STEP_MACRO, VB, ROWS_INTERIOR, PHASE><<<grid, block, 0, s>>>(a);
+                break;
+            case MODE_REDUCE: aa_kernel<LBM_S, MODE_REDUCE, VB, ROWS_INTERIOR, PHASE><<<grid, block, 0, s>>>(a); break;
+            default: return cudaErrorInvalidValue;
+            }
+        } else {
+            switch (mode) {
+            case MODE_STEP: aa_kernel<LBM_S, MODE_STEP, VB, ROWS_FACES, PHASE><<<grid, block, 0, s>>>(a); break;
+            case MODE_STEP_MACRO:
+                aa_kernel<LBM_S, MODE_STEP_MACRO, VB, ROWS_FACES, PHASE><<<grid, block, 0, s>>>(a);
+                break;
+            case MODE_REDUCE: aa_kernel<LBM_S, MODE_REDUCE, VB, ROWS_FACES, PHASE><<<grid, block, 0, s>>>(a); break;
+            default: return cudaErrorInvalidValue;
+            }
+        }
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    if (nparts) *nparts = gi + gf;
+    return cudaSuccess;
+}
+
+// AA variant: 8-byte vectors for FP32 (its fastest two-lattice width), 16-byte
+// otherwise; a.aa_phase picks the A- or B-step.
+cudaError_t LBM_CAT(launch_aa_, LBM_SFX)(int mode, const StepArgs &a, unsigned block, cudaStream_t s,
+                                         unsigned *nparts)
+{
+    constexpr int VB = sizeof(LBM_S) == 4 ? 8 : 16;
+    return a.aa_phase ? launch_aa_phase<VB, 1>(mode, a, block, s, nparts)
+                      : launch_aa_phase<VB, 0>(mode, a, block, s, nparts);
+}
+
 cudaError_t LBM_CAT(launch_pull_, LBM_SFX)(int mode, const StepArgs &a, unsigned block, cudaStream_t s,
                                            unsigned *nparts)
 {

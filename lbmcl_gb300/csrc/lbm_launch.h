@@ -16,6 +16,8 @@ struct DumpArgs;
     cudaError_t launch_pull_##SFX(int mode, const StepArgs &a, unsigned block, cudaStream_t s,       \
                                   unsigned *nparts);                                                 \
     cudaError_t launch_narrow_##SFX(int mode, const StepArgs &a, unsigned block, cudaStream_t s);    \
+    cudaError_t launch_aa_##SFX(int mode, const StepArgs &a, unsigned block, cudaStream_t s,         \
+                                unsigned *nparts);                                                   \
     cudaError_t launch_staged_##SFX(int mode, const StepArgs &a, unsigned grid, unsigned block,      \
                                     size_t smem, cudaStream_t s);                                    \
     const void *staged_kernel_ptr_##SFX(int mode);                                                  \

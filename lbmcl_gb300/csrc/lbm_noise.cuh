@@ -81,12 +81,22 @@ __device__ __forceinline__ void gauss_pair(uint64_t seed, uint64_t site, uint32_
     for (uint32_t block = 0; block < 16; ++block) {
         uint32_t c[4] = {(uint32_t)site, (uint32_t)(site >> 32), pair, block};
         philox4x32_10(c, k0, k1);
+        // the first accepted attempt of the four, found by selects; the
+        // logarithm, division and square root then run once
+        float v1 = 0.0f, v2 = 0.0f, s = 0.0f;
+        bool found = false;
 #pragma unroll
-        for (int a = 0; a < 4; ++a) {
-            const float v1 = sym_uniform16(c[a] & 0xffffu);
-            const float v2 = sym_uniform16(c[a] >> 16);
-            const float s = __fadd_rn(__fmul_rn(v1, v1), __fmul_rn(v2, v2));
-            if (s >= 1.0f || s == 0.0f) continue;
+        for (int a = 3; a >= 0; --a) {
+            const float w1 = sym_uniform16(c[a] & 0xffffu);
+            const float w2 = sym_uniform16(c[a] >> 16);
+            const float sa = __fadd_rn(__fmul_rn(w1, w1), __fmul_rn(w2, w2));
+            const bool ok = sa < 1.0f && sa != 0.0f;
+            v1 = ok ? w1 : v1;
+            v2 = ok ? w2 : v2;
+            s = ok ? sa : s;
+            found |= ok;
+        }
+        if (found) {
             const float t = __fdiv_rn(__fmul_rn(-2.0f, series_logf(s)), s);
             const float r = __fsqrt_rn(t);
             z0 = __fmul_rn(v1, r);

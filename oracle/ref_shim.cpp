@@ -77,15 +77,25 @@ void ref_initialize(real_t *f_stream, real_t *f_collide, real_t *density, real_t
             }
 }
 
-void ref_compute(real_t *f_stream, const real_t *f_collide, real_t *density, real_t *u,
-                 const int *map, int update_macro)
+// One reference step over the z-planes [z0, z1), the planes split over the
+// OpenMP threads: every site pushes into distinct slots (kernels.cl:420-424),
+// so the planes are independent; get_global_id reads a thread-local index.
+void ref_compute_slab(real_t *f_stream, const real_t *f_collide, real_t *density, real_t *u,
+                      const int *map, int update_macro, int z0, int z1)
 {
-    for (int z = 0; z < g_dim; ++z)
+#pragma omp parallel for schedule(static)
+    for (int z = z0; z < z1; ++z)
         for (int y = 0; y < g_dim; ++y)
             for (int x = 0; x < g_dim; ++x) {
                 g_gid[0] = x; g_gid[1] = y; g_gid[2] = z;
                 compute(f_stream, f_collide, density, u, map, update_macro);
             }
+}
+
+void ref_compute(real_t *f_stream, const real_t *f_collide, real_t *density, real_t *u,
+                 const int *map, int update_macro)
+{
+    ref_compute_slab(f_stream, f_collide, density, u, map, update_macro, 0, g_dim);
 }
 
 int ref_real_size(void) { return (int)sizeof(real_t); }

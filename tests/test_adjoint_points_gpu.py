@@ -73,18 +73,25 @@ def test_full_states_on_request_and_switching_paths(capi):
     np.testing.assert_array_equal(full[2], ref[2])
     np.testing.assert_array_equal(full[3], ref[3])
     lid, target = case(dim, dim + iters)
+    out = []
     with capi.Lattice(dim, velocity=0.0, precision="fp32", lid=lid, tau=0.53, seed=3, noise_sigma=1e-4,
                       adjoint_steps=1) as L:
         L.adjoint_set_loss(dim // 2, target)
         f0 = L.f()
-        out = []
+        # R_0 loaded explicitly each time: no lid dependence through the init
         for want_tau in (False, True, False, True):
             L.load_f(f0)
             L.adjoint_forward(iters, every)
             out.append(L.adjoint_backward(1.0, want_tau=want_tau))
+    with capi.Lattice(dim, velocity=0.0, precision="fp32", lid=lid, tau=0.53, adjoint_steps=1) as L:
+        L.adjoint_set_loss(dim // 2, target)
+        L.load_f(f0)
+        L.adjoint_forward(iters, every)
+        fresh = L.adjoint_backward(1.0, want_tau=True)
     np.testing.assert_array_equal(out[0][1], out[2][1])
     np.testing.assert_array_equal(out[1][1], out[3][1])
-    np.testing.assert_array_equal(out[1][1], ref[2])
+    np.testing.assert_array_equal(out[1][1], fresh[1])
+    np.testing.assert_array_equal(out[1][2], fresh[2])
 
 
 def _init_bytes_fp32(dim, block=128):

@@ -55,67 +55,57 @@ def test_rejects_oversized_work_group(lbmcl_bin):
     assert r.returncode == 255 and "Please enter a good work_group_size" in r.stderr
 
 
-# -------------------------------------------------------- renderers ------
-def render_f_dump(f, dim, stride):
-    """lbmcl.hpp:206-258 for one CSoA buffer."""
-    dd = len(str(dim)) if dim > 0 else 1
-    head = " " * (dd * 3 + 5) + "".join("%8d " % q for q in range(19)) + "\n"
-    out = []
-    for z in range(dim):
-        for y in range(dim):
-            out.append(head)
-            for x in range(dim):
-                i = x + y * dim + z * dim * dim
-                vals = "".join("%8.6f " % float(f[((i // stride) * 19 + q) * stride + (i & (stride - 1))])
-                               for q in range(19))
-                out.append(("(".rjust(dd)) + "%d,%d,%d) " % (x, y, z) + vals + "\n")
-            out.append("\n")
-        out.append("\n")
-    out.append("\n")
-    return "".join(out)
+# ------------------------------------------- the reference's own writers ------
+def _digest_runs():
+    import json
+    with open(os.path.join(GOLD, "host_digests.json")) as fh:
+        return json.load(fh)["runs"]
 
 
-def render_map(cmap, dim):
-    """lbmcl.hpp:159-203."""
-    def code(c):
-        v = 0
-        if c == 0x1: v = 1
-        if c & 0x2: v = 2
-        if c & 0x3F0: v = 3
-        if c == 0x8: v = 4
-        if c == 0x4: v = 5
-        return v
-    out = ["# FLUID       1\n# MOVING      2\n# BOUNDARY    3\n# WALL        4\n# CORNER      5\n\n"]
-    for z in range(dim):
-        for y in range(dim):
-            out.append("".join("%d " % code(cmap[x + y * dim + z * dim * dim]) for x in range(dim)) + "\n")
-        out.append("\n")
-    out.append("\n")
-    return "".join(out)
+def test_digests_come_from_the_reference_writers(tmp_path):
+    """Where the reference tree was present at build time (oracle/_ref), the
+    committed digests are re-derived from the reference's own writers fed
+    with the oracle's data (tests/golden/make_host_golden.py)."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("make_host_golden", os.path.join(GOLD, "make_host_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    if not os.path.exists(mg.LIB):
+        pytest.skip("the reference writers are built only where the reference tree is present")
+    assert mg.generate()["runs"] == _digest_runs()
 
 
 # ---------------------------------------------------------------- GPU ------
 @pytest.mark.gpu
-def test_make_test8_files_byte_identical(lbmcl_bin, oracle, tmp_path, capi):
-    """make testall at 8^3 (-f -m, every iteration): f_<it>.dump, map.dump and
-    lbmcl.<it>.vti equal the reference's files for the same run (rendered
-    from the oracle, which is bit-identical to the reference kernel)."""
+@pytest.mark.parametrize("k", range(3))
+def test_output_files_equal_the_reference_writers(lbmcl_bin, tmp_path, capi, k):
+    """For each run (make testall at 8^3 with f and map dumps, an FP64 run
+    with f dumps, a 32^3 test32-like run) every file the lbmcl program
+    writes has the SHA-256 of the file the reference's own writers
+    (lbmcl.hpp:159-334, compiled against an OpenCL stand-in) write for the
+    same run, and no file is missing or extra."""
+    import hashlib
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("make_host_golden", os.path.join(GOLD, "make_host_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    entry = _digest_runs()[k]
+    r = run(lbmcl_bin, *mg.cli_args(entry["run"], tmp_path, tmp_path))
+    assert r.returncode == 0, r.stderr
+    got = {f.name: hashlib.sha256(f.read_bytes()).hexdigest() for f in sorted(tmp_path.iterdir())}
+    assert sorted(got) == sorted(entry["files"])
+    bad = [f for f in got if got[f] != entry["files"][f]]
+    assert not bad, bad
+
+
+@pytest.mark.gpu
+def test_make_test8_against_golden(lbmcl_bin, tmp_path, capi):
+    """make test8 (Makefile:73-78): the VTI files against the reference's
+    golden Sailfish data, with verify.py's metrics."""
     from lbmcl_gb300 import vti
     r = run(lbmcl_bin, "-d", 8, "-n", 0.0089, "-u", 0.05, "-i", 10, "-e", 1, "-w", "8,8,8", "-s", 8,
-            "-v", tmp_path, "-p", tmp_path, "-f", "-m")
+            "-v", tmp_path)
     assert r.returncode == 0, r.stderr
-    o = oracle.OracleLattice(8, 0.0089, 0.05, "f32", 8)
-    assert (tmp_path / "map.dump").read_text() == render_map(o.map, 8)
-    ref_vti = tmp_path / "ref.vti"
-    vti.write_vti_ascii(str(ref_vti), 8, o.rho, o.u)
-    assert (tmp_path / "lbmcl.00.vti").read_text() == ref_vti.read_text()
-    assert (tmp_path / "f_00.dump").read_text() == render_f_dump(o.state, 8, 8)
-    for it in range(1, 11):
-        # f_<it> is the buffer iteration it reads (lbmcl.hpp:517-519)
-        assert (tmp_path / f"f_{it:02d}.dump").read_text() == render_f_dump(o.state, 8, 8), it
-        o.step(1, every=1)
-        vti.write_vti_ascii(str(ref_vti), 8, o.rho, o.u)
-        assert (tmp_path / f"lbmcl.{it:02d}.vti").read_text() == ref_vti.read_text(), it
     g8 = np.load(os.path.join(GOLD, "sailfish_ldc8.npz"))
     for it in range(0, 11):
         got = vti.read_vti(str(tmp_path / f"lbmcl.{it:02d}.vti"))
@@ -140,15 +130,8 @@ def test_make_test32_against_golden(lbmcl_bin, tmp_path, capi):
 
 
 @pytest.mark.gpu
-def test_double_and_sixteen_bit_runs(lbmcl_bin, oracle, tmp_path, capi):
+def test_sixteen_bit_runs(lbmcl_bin, tmp_path, capi):
     from lbmcl_gb300 import vti
-    r = run(lbmcl_bin, "-d", 16, "-i", 7, "-e", 7, "-F", "-s", 16, "-v", tmp_path)
-    assert r.returncode == 0, r.stderr
-    o = oracle.OracleLattice(16, 0.0089, 0.05, "f64", 16)
-    o.step(7, every=7)
-    ref_vti = tmp_path / "ref.vti"
-    vti.write_vti_ascii(str(ref_vti), 16, o.rho, o.u)
-    assert (tmp_path / "lbmcl.7.vti").read_text() == ref_vti.read_text()
     for p in ("fp16", "bf16"):
         d = tmp_path / p
         d.mkdir()

@@ -35,13 +35,14 @@ def test_map_bit_exact(capi, oracle, dim):
         np.testing.assert_array_equal(L.cell_map(), oracle.cell_types(dim))
 
 
-@pytest.mark.parametrize("kernel", ["direct", "staged"])
+@pytest.mark.parametrize("kernel", ["direct", "staged", "aa"])
 @pytest.mark.parametrize("prec", ["f32", "f64"])
 @pytest.mark.parametrize("dim,stride", [(8, 8), (32, 8), (16, 1), (16, 4096), (4, 4), (12, 16)])
 def test_f_after_each_step(capi, oracle, prec, dim, stride, kernel):
     """Config 1 shape (32^3, stride 8, 10 steps) and layout / size variations:
     the full post-stream buffer, wall slots included, after every iteration,
-    for both iteration-kernel variants."""
+    for the iteration-kernel variants (the in-place AA one in both of its
+    layouts)."""
     o = oracle.OracleLattice(dim, 0.0089, 0.05, prec, stride)
     with capi.Lattice(dim, 0.0089, 0.05, precision=GPU_PREC[prec], stride=stride, kernel=kernel) as L:
         assert_f_close(L.f(), o.state, TOL[prec], "initial")
@@ -55,7 +56,7 @@ def test_f_after_each_step(capi, oracle, prec, dim, stride, kernel):
             np.testing.assert_array_equal(bits(L.u()), bits(o.u))
 
 
-@pytest.mark.parametrize("kernel", ["direct", "staged"])
+@pytest.mark.parametrize("kernel", ["direct", "staged", "aa"])
 @pytest.mark.parametrize("prec", ["f32", "f64"])
 def test_lid_profile_noise_and_macro_every(capi, oracle, prec, kernel):
     """Per-column lid, seeded noise on FLUID populations, macros every 3rd
@@ -99,7 +100,7 @@ def test_golden_sailfish_8_and_32(capi):
             assert c["mae_rho"] < 5e-6 and c["mae_v"] < 2e-6, (it, c)
 
 
-@pytest.mark.parametrize("kernel", ["direct", "staged"])
+@pytest.mark.parametrize("kernel", ["direct", "staged", "aa"])
 @pytest.mark.parametrize("prec", ["f32", "f64"])
 def test_64cube_200_steps(capi, oracle, prec, kernel):
     o = oracle.OracleLattice(64, 0.0089, 0.05, prec, 64, seed=7, noise_sigma=1e-4)
@@ -112,10 +113,13 @@ def test_64cube_200_steps(capi, oracle, prec, kernel):
         assert np.array_equal(bits(g), bits(o.state))
 
 
+@pytest.mark.parametrize("kernel,steps", [("auto", 5), ("aa", 5), ("aa", 6)])
 @pytest.mark.parametrize("prec", ["fp32", "fp64", "fp16", "bf16"])
-def test_load_dump_round_trip(capi, prec):
-    with capi.Lattice(16, precision=prec, stride=16, seed=3, noise_sigma=1e-4) as L:
-        L.step(5)
+def test_load_dump_round_trip(capi, prec, kernel, steps):
+    """F dump / load and raw dump / load round trips (the in-place AA lattice
+    in both of its layouts)."""
+    with capi.Lattice(16, precision=prec, stride=16, seed=3, noise_sigma=1e-4, kernel=kernel) as L:
+        L.step(steps)
         f0 = L.f()
         raw = L.raw()
         L.load_f(f0)
@@ -129,12 +133,15 @@ def test_load_dump_round_trip(capi, prec):
         np.testing.assert_array_equal(L.raw(), raw)
 
 
+@pytest.mark.parametrize("kernel,pre", [("auto", 0), ("aa", 0), ("aa", 1)])
 @pytest.mark.parametrize("prec", ["f32", "f64"])
-def test_load_then_continue(capi, oracle, prec):
-    """A state loaded from the host continues exactly like the oracle."""
+def test_load_then_continue(capi, oracle, prec, kernel, pre):
+    """A state loaded from the host continues exactly like the oracle (into
+    an AA lattice in either layout)."""
     o = oracle.OracleLattice(16, 0.0089, 0.05, prec, 8, seed=5, noise_sigma=1e-4)
     o.step(7, every=0)
-    with capi.Lattice(16, 0.0089, 0.05, precision=GPU_PREC[prec], stride=8) as L:
+    with capi.Lattice(16, 0.0089, 0.05, precision=GPU_PREC[prec], stride=8, kernel=kernel) as L:
+        L.step(pre)
         L.load_f(o.state)
         assert np.array_equal(bits(L.f()), bits(o.state))
         o.step(5, every=5)
@@ -142,13 +149,15 @@ def test_load_then_continue(capi, oracle, prec):
         assert np.array_equal(bits(L.f()), bits(o.state))
 
 
+@pytest.mark.parametrize("kernel,steps", [("auto", 25), ("aa", 25), ("aa", 24)])
 @pytest.mark.parametrize("prec", ["f32", "f64"])
-def test_reduce_matches_oracle_moments(capi, oracle, prec):
+def test_reduce_matches_oracle_moments(capi, oracle, prec, kernel, steps):
     dim = 32
     o = oracle.OracleLattice(dim, 0.0089, 0.05, prec, 32, seed=1, noise_sigma=1e-4)
-    with capi.Lattice(dim, 0.0089, 0.05, precision=GPU_PREC[prec], stride=32, seed=1, noise_sigma=1e-4) as L:
-        o.step(25, every=0)
-        L.step(25, every=0)
+    with capi.Lattice(dim, 0.0089, 0.05, precision=GPU_PREC[prec], stride=32, seed=1, noise_sigma=1e-4,
+                      kernel=kernel) as L:
+        o.step(steps, every=0)
+        L.step(steps, every=0)
         mass, energy, count = L.reduce()
     # the moments of the current state are what the next iteration stores
     o.step(1, every=1)
@@ -221,7 +230,7 @@ def test_kernel_variants_agree(capi, prec, dim, stages):
     """The iteration kernels move data differently but run the same site
     update: their populations and macros agree bit for bit."""
     outs = []
-    for kernel in ("direct", "staged", "narrow"):
+    for kernel in ("direct", "staged", "narrow", "aa"):
         with capi.Lattice(dim, 0.005, 0.08, precision=prec, seed=21, noise_sigma=1e-4, kernel=kernel,
                           stages=stages) as L:
             L.step(7)
@@ -257,7 +266,8 @@ def test_graph_replay_matches_direct_launches(capi, prec, nsteps, every):
 
 
 @pytest.mark.parametrize("prec,kernel", [("fp32", "direct"), ("fp32", "staged"), ("fp16", "narrow"),
-                                         ("fp16", "staged"), ("bf16", "direct")])
+                                         ("fp16", "staged"), ("bf16", "direct"), ("fp32", "aa"), ("fp16", "aa"),
+                                         ("fp64", "aa")])
 def test_graph_replay_every_kernel_variant(capi, prec, kernel):
     """Graph replay of each iteration-kernel variant (the staged one with its
     mbarrier ring and dynamic shared memory) equals its direct launches."""
@@ -270,3 +280,51 @@ def test_graph_replay_every_kernel_variant(capi, prec, kernel):
             res.append((L.f(), L.rho(), L.u()))
     for a, b in zip(*res):
         np.testing.assert_array_equal(a.view(np.uint8), b.view(np.uint8))
+
+
+@pytest.mark.parametrize("prec", ["fp32", "fp16", "bf16", "fp64"])
+@pytest.mark.parametrize("dim", [8, 40, 136])
+def test_in_place_variant_matches_two_lattices_every_step(capi, prec, dim):
+    """The AA lattice (one buffer, alternating local and neighbour steps)
+    against the default two-lattice kernels after every iteration of both
+    kinds, macro iterations included: bit for bit.  dim 136 gives rows that
+    start inside a warp (17 vectors of 8 sites)."""
+    outs = {}
+    for kernel in ("auto", "aa"):
+        res = []
+        with capi.Lattice(dim, 0.005, 0.08, precision=prec, seed=13, noise_sigma=1e-4, kernel=kernel,
+                          graph_iterations=1) as L:
+            res.append(L.f())
+            for it in range(1, 8):
+                L.step(1, every=3)
+                res.append((L.f(), L.rho(), L.u()))
+        outs[kernel] = res
+    np.testing.assert_array_equal(bits(outs["auto"][0]), bits(outs["aa"][0]))
+    for a, b in zip(outs["auto"][1:], outs["aa"][1:]):
+        for x, y in zip(a, b):
+            np.testing.assert_array_equal(bits(x), bits(y))
+
+
+def test_in_place_variant_memory_and_adjoint_refusal(capi):
+    """The AA handle holds one population lattice (its budget check counts
+    one), and the gradient calls refuse it with a status and a message."""
+    import ctypes as C
+    dim = 32
+    fbytes = 19 * dim ** 3 * 4
+    with capi.Lattice(dim, precision="fp32", kernel="aa") as L:
+        L.adjoint_set_loss(16, None)
+        J = C.c_double()
+        assert capi.lib().lbm_adjoint_forward(L.h, 4, 4, C.byref(J)) == capi.ESTATE
+        assert "two-lattice" in capi.lib().lbm_last_error().decode()
+        L.step(3)
+        L.sync()
+    # a budget between the one-lattice and the two-lattice needs: only AA fits
+    n = dim ** 3
+    nvec = (dim // 4) * (dim - 2) ** 2
+    two = (2 * fbytes + n + 16 * n + dim * dim * 4 + min(1 << 25, 19 * n) * 4 + (-(-nvec // 128) + 2) * 16 +
+           4 * 8 + 4)  # lbm_init's need of a two-lattice FP32 handle
+    with pytest.raises(capi.LbmError):
+        capi.Lattice(dim, precision="fp32", max_device_bytes=two - fbytes // 2)
+    with capi.Lattice(dim, precision="fp32", kernel="aa", max_device_bytes=two - fbytes // 2) as L:
+        L.step(2)
+        L.sync()
