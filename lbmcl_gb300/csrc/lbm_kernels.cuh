@@ -22,6 +22,17 @@
 #include "lbm_device.cuh"
 #include "lbm_noise.cuh"
 
+// x-shifted neighbours of the pull kernel's loads from the neighbouring lane
+// (1) or from memory (0)
+#ifndef LBM_HALO_SHFL
+#define LBM_HALO_SHFL 1
+#endif
+// 16-bit storage: macro / linearisation-point stores of four sites at a time
+// (1) or of pairs (0)
+#ifndef LBM_QUAD_STORES
+#define LBM_QUAD_STORES 1
+#endif
+
 namespace lbm {
 
 template <class S> struct Compute { using type = float; };
@@ -75,6 +86,22 @@ template <class S> __device__ __forceinline__ S zero_elem()
     return s;
 }
 
+// One storage element from lane +-delta (up: from the lower lane).
+template <class S> __device__ __forceinline__ S shfl_elem(S v, int delta, bool up, unsigned mask = 0xffffffffu)
+{
+    if constexpr (sizeof(S) == 2) {
+        unsigned short u;
+        memcpy(&u, &v, 2);
+        const int r = up ? __shfl_up_sync(mask, (int)u, delta) : __shfl_down_sync(mask, (int)u, delta);
+        const unsigned short ur = (unsigned short)r;
+        S o;
+        memcpy(&o, &ur, 2);
+        return o;
+    } else {
+        return up ? __shfl_up_sync(mask, v, delta) : __shfl_down_sync(mask, v, delta);
+    }
+}
+
 // Pull one population for the V sites x0..x0+V-1 of a row: the values at
 // x - EX.  `row` points at x = 0 of the source row.
 template <class S, int V, int EX>
@@ -94,6 +121,42 @@ __device__ __forceinline__ void gather_row(const S *__restrict__ row, int x0, in
         for (int k = 0; k < V - 1; ++k) out[k] = v[k + 1];
         out[V - 1] = (x0 + V < dim) ? load_one(row + x0 + V) : zero_elem<S>();
     }
+}
+
+// As gather_row, with the element just outside the vector taken from the
+// neighbouring lane, which holds the neighbouring vector of the same row when
+// it runs this code (`mask`, rows of consecutive threads): a real load only
+// at a warp's edge.
+template <class S, int V, int EX>
+__device__ __forceinline__ void gather_row_lanes(const S *__restrict__ row, int x0, int dim, S (&out)[V],
+                                                 unsigned mask, int lane)
+{
+    S v[V];
+    load_vec<S, V>(row + x0, v);
+    if constexpr (EX == 0) {
+#pragma unroll
+        for (int k = 0; k < V; ++k) out[k] = v[k];
+    } else if constexpr (EX == 1) {
+        const S nb = shfl_elem(v[V - 1], 1, true, mask);
+        out[0] = (x0 == 0) ? zero_elem<S>() : (lane > 0 ? nb : load_one(row + x0 - 1));
+#pragma unroll
+        for (int k = 1; k < V; ++k) out[k] = v[k - 1];
+    } else {
+        const S nb = shfl_elem(v[0], 1, false, mask);
+#pragma unroll
+        for (int k = 0; k < V - 1; ++k) out[k] = v[k + 1];
+        const bool next = lane < 31 && ((mask >> (lane + 1)) & 1u);
+        out[V - 1] = (x0 + V >= dim) ? zero_elem<S>() : (next ? nb : load_one(row + x0 + V));
+    }
+}
+
+template <class S, int V, int I>
+__device__ __forceinline__ void gather_all_lanes(const S *__restrict__ fin, size_t n, size_t rowoff, int dim, int x0,
+                                                 S (&fs)[Q][V], unsigned mask, int lane)
+{
+    const ptrdiff_t shift = (ptrdiff_t)ez_of(I) * dim * dim + (ptrdiff_t)ey_of(I) * dim;
+    gather_row_lanes<S, V, ex_of(I)>(fin + (size_t)I * n + rowoff - shift, x0, dim, fs[I], mask, lane);
+    if constexpr (I + 1 < Q) gather_all_lanes<S, V, I + 1>(fin, n, rowoff, dim, x0, fs, mask, lane);
 }
 
 template <int V> struct MapWord;
@@ -431,6 +494,36 @@ __device__ __forceinline__ void store_macro_pair(const StepArgs &a, size_t id, b
     }
 }
 
+// rho / u (MODE_STEP_MACRO) or the FLUID linearisation point (MODE_STEP_ADJ)
+// of four neighbouring FLUID sites (id a multiple of 4, FP32 macro type):
+// the first pair's values held as floats (h: r0 r1 ux0 ux1 uy0 uy1 uz0 uz1),
+// one 16-byte store per field when all four store (`all`), else per site
+template <int MODE>
+__device__ __forceinline__ void store_macro_quad(const StepArgs &a, size_t id, bool all, const float (&h)[8],
+                                                 bool s0, bool s1, const SiteOut &o2, const SiteOut &o3, bool s2,
+                                                 bool s3)
+{
+    float *u = static_cast<float *>(a.u);
+    float *rho = static_cast<float *>(a.rho);
+    if (all) {
+        if (MODE == MODE_STEP_MACRO)
+            *reinterpret_cast<float4 *>(rho + id) = make_float4(h[0], h[1], (float)o2.r, (float)o3.r);
+        *reinterpret_cast<float4 *>(u + id) = make_float4(h[2], h[3], (float)o2.ux, (float)o3.ux);
+        *reinterpret_cast<float4 *>(u + a.n + id) = make_float4(h[4], h[5], (float)o2.uy, (float)o3.uy);
+        *reinterpret_cast<float4 *>(u + 2 * a.n + id) = make_float4(h[6], h[7], (float)o2.uz, (float)o3.uz);
+        return;
+    }
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+        if (!(j ? s1 : s0)) continue;
+        if (MODE == MODE_STEP_MACRO) rho[id + j] = h[j];
+        u[id + j] = h[2 + j];
+        u[a.n + id + j] = h[4 + j];
+        u[2 * a.n + id + j] = h[6 + j];
+    }
+    store_macro_pair<float, MODE>(a, id + 2, s2, s3, o2, o3);
+}
+
 __device__ __forceinline__ void accumulate(const SiteOut &o, double &m, double &e)
 {
     m += o.r;
@@ -527,6 +620,8 @@ __device__ __forceinline__ void update_vector(S (&fs)[Q][V], typename MapWord<V>
         if (FLUID_ONLY || mw == 0) {
             // all V sites FLUID (the bulk of the lattice): no per-site branches,
             // two sites per step so the output converts as packed pairs
+            float hq[8];
+            bool qf0 = false, qf1 = false;
 #pragma unroll
             for (int k = 0; k < V; k += 2) {
                 float D0[Q], D1[Q];
@@ -546,8 +641,26 @@ __device__ __forceinline__ void update_vector(S (&fs)[Q][V], typename MapWord<V>
                 const bool f0 = !FLUID_ONLY || (unsigned)(x0 + k - 2) <= (unsigned)(dim - 5);
                 const bool f1 = !FLUID_ONLY || (unsigned)(x0 + k - 1) <= (unsigned)(dim - 5);
                 bad |= (f0 && o0.bad) || (f1 && o1.bad);
-                if constexpr (MODE == MODE_STEP_MACRO || MODE == MODE_STEP_ADJ)
+                if constexpr ((MODE == MODE_STEP_MACRO || MODE == MODE_STEP_ADJ) && V % 4 == 0 && LBM_QUAD_STORES) {
+                    // four sites per 16-byte store: the first pair waits in
+                    // registers for the second
+                    if ((k & 2) == 0) {
+                        hq[0] = (float)o0.r;
+                        hq[1] = (float)o1.r;
+                        hq[2] = (float)o0.ux;
+                        hq[3] = (float)o1.ux;
+                        hq[4] = (float)o0.uy;
+                        hq[5] = (float)o1.uy;
+                        hq[6] = (float)o0.uz;
+                        hq[7] = (float)o1.uz;
+                        qf0 = f0;
+                        qf1 = f1;
+                    } else {
+                        store_macro_quad<MODE>(a, site0 + k - 2, qf0 && qf1 && f0 && f1, hq, qf0, qf1, o0, o1, f0, f1);
+                    }
+                } else if constexpr (MODE == MODE_STEP_MACRO || MODE == MODE_STEP_ADJ) {
                     store_macro_pair<C, MODE>(a, site0 + k, f0, f1, o0, o1);
+                }
                 if (MODE == MODE_REDUCE) {
                     if (f0) accumulate(o0, red_m, red_e);
                     if (f1) accumulate(o1, red_m, red_e);
@@ -590,8 +703,11 @@ __device__ __forceinline__ void face_fix(const StepArgs &a, size_t rowoff, int x
     }
 }
 
+// mask != 0: the threads in `mask` run this together (rows of consecutive
+// threads), and x-shifted neighbours come from the neighbouring lanes
 template <class S, int MODE, int V, bool INTERIOR>
-__device__ __forceinline__ void pull_vector(const StepArgs &a, int xv, int y, int z, double &red_m, double &red_e)
+__device__ __forceinline__ void pull_vector(const StepArgs &a, int xv, int y, int z, double &red_m, double &red_e,
+                                            unsigned mask = 0)
 {
     const int dim = a.dim;
     const int x0 = xv * V;
@@ -601,7 +717,8 @@ __device__ __forceinline__ void pull_vector(const StepArgs &a, int xv, int y, in
     if (!INTERIOR) mw = __ldg(reinterpret_cast<const typename MapWord<V>::type *>(a.map + site0));
     const S *__restrict__ fin = static_cast<const S *>(a.fin);
     S fs[Q][V];
-    gather_all<S, V, 0>(fin, a.n, rowoff, dim, x0, fs);
+    if (LBM_HALO_SHFL && mask) gather_all_lanes<S, V, 0>(fin, a.n, rowoff, dim, x0, fs, mask, (int)(threadIdx.x & 31));
+    else gather_all<S, V, 0>(fin, a.n, rowoff, dim, x0, fs);
     update_vector<S, MODE, V, INTERIOR>(fs, mw, a, y, z, x0, site0, red_m, red_e);
     if (INTERIOR && MODE != MODE_REDUCE) {
         // the walls (x = 0, dim-1) hold values nobody reads; the faces bounce back
@@ -685,7 +802,9 @@ __global__ void __launch_bounds__(LBM_PULL_MAXT, min_blocks<S, VB>()) pull_kerne
     double red_m = 0.0, red_e = 0.0;
     const unsigned nrows = ROWS == ROWS_INTERIOR ? (unsigned)(a.dim - 4) * (unsigned)(a.dim - 4)
                                                  : 4u * (unsigned)(a.dim - 3);
-    if (g < nrows * (unsigned)a.nvx) {
+    const bool active = g < nrows * (unsigned)a.nvx;
+    const unsigned mask = __ballot_sync(0xffffffffu, active);
+    if (active) {
         const int dim = a.dim;
         const unsigned row = g / (unsigned)a.nvx;
         const int xv = (int)(g - row * (unsigned)a.nvx);
@@ -696,7 +815,7 @@ __global__ void __launch_bounds__(LBM_PULL_MAXT, min_blocks<S, VB>()) pull_kerne
         } else {
             decode_face_row(dim, row, y, z);
         }
-        pull_vector<S, MODE, V, ROWS == ROWS_INTERIOR>(a, xv, y, z, red_m, red_e);
+        pull_vector<S, MODE, V, ROWS == ROWS_INTERIOR>(a, xv, y, z, red_m, red_e, mask);
     }
     if (MODE == MODE_REDUCE) block_reduce_write(red_m, red_e, a.partials + 2 * (size_t)a.partial_base);
 }
@@ -719,21 +838,6 @@ __global__ void __launch_bounds__(LBM_PULL_MAXT, min_blocks<S, VB>()) pull_kerne
 // source is a wall (or outside the lattice) and in wall-sourced slots of
 // boundary sites: slots that no iteration and no dump reads.
 // ---------------------------------------------------------------------------
-template <class S> __device__ __forceinline__ S shfl_elem(S v, int delta, bool up)
-{
-    if constexpr (sizeof(S) == 2) {
-        unsigned short u;
-        memcpy(&u, &v, 2);
-        const int r = up ? __shfl_up_sync(0xffffffffu, (int)u, delta) : __shfl_down_sync(0xffffffffu, (int)u, delta);
-        const unsigned short ur = (unsigned short)r;
-        S o;
-        memcpy(&o, &ur, 2);
-        return o;
-    } else {
-        return up ? __shfl_up_sync(0xffffffffu, v, delta) : __shfl_down_sync(0xffffffffu, v, delta);
-    }
-}
-
 // out[k] (site x0 + k) to position x0 + k + EX of a row (`row` at x = 0).
 // Every lane of the warp calls this (the shuffles); inactive lanes store
 // nothing.
