@@ -670,7 +670,7 @@ __global__ void __launch_bounds__(ADJ2_EX * ADJ2_EY, MACRO ? LBM_ADJ2M_MINB : LB
 // tiles, plane slots and arithmetic as adjoint2_kernel<S, true>.
 // ---------------------------------------------------------------------------
 #ifndef LBM_ADJ2P_MINB
-#define LBM_ADJ2P_MINB 2
+#define LBM_ADJ2P_MINB 3
 #endif
 
 template <class S>

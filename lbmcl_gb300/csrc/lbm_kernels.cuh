@@ -22,11 +22,6 @@
 #include "lbm_device.cuh"
 #include "lbm_noise.cuh"
 
-// x-shifted neighbours of the pull kernel's loads from the neighbouring lane
-// (1) or from memory (0)
-#ifndef LBM_HALO_SHFL
-#define LBM_HALO_SHFL 1
-#endif
 // 16-bit storage: macro / linearisation-point stores of four sites at a time
 // (1) or of pairs (0)
 #ifndef LBM_QUAD_STORES
@@ -121,42 +116,6 @@ __device__ __forceinline__ void gather_row(const S *__restrict__ row, int x0, in
         for (int k = 0; k < V - 1; ++k) out[k] = v[k + 1];
         out[V - 1] = (x0 + V < dim) ? load_one(row + x0 + V) : zero_elem<S>();
     }
-}
-
-// As gather_row, with the element just outside the vector taken from the
-// neighbouring lane, which holds the neighbouring vector of the same row when
-// it runs this code (`mask`, rows of consecutive threads): a real load only
-// at a warp's edge.
-template <class S, int V, int EX>
-__device__ __forceinline__ void gather_row_lanes(const S *__restrict__ row, int x0, int dim, S (&out)[V],
-                                                 unsigned mask, int lane)
-{
-    S v[V];
-    load_vec<S, V>(row + x0, v);
-    if constexpr (EX == 0) {
-#pragma unroll
-        for (int k = 0; k < V; ++k) out[k] = v[k];
-    } else if constexpr (EX == 1) {
-        const S nb = shfl_elem(v[V - 1], 1, true, mask);
-        out[0] = (x0 == 0) ? zero_elem<S>() : (lane > 0 ? nb : load_one(row + x0 - 1));
-#pragma unroll
-        for (int k = 1; k < V; ++k) out[k] = v[k - 1];
-    } else {
-        const S nb = shfl_elem(v[0], 1, false, mask);
-#pragma unroll
-        for (int k = 0; k < V - 1; ++k) out[k] = v[k + 1];
-        const bool next = lane < 31 && ((mask >> (lane + 1)) & 1u);
-        out[V - 1] = (x0 + V >= dim) ? zero_elem<S>() : (next ? nb : load_one(row + x0 + V));
-    }
-}
-
-template <class S, int V, int I>
-__device__ __forceinline__ void gather_all_lanes(const S *__restrict__ fin, size_t n, size_t rowoff, int dim, int x0,
-                                                 S (&fs)[Q][V], unsigned mask, int lane)
-{
-    const ptrdiff_t shift = (ptrdiff_t)ez_of(I) * dim * dim + (ptrdiff_t)ey_of(I) * dim;
-    gather_row_lanes<S, V, ex_of(I)>(fin + (size_t)I * n + rowoff - shift, x0, dim, fs[I], mask, lane);
-    if constexpr (I + 1 < Q) gather_all_lanes<S, V, I + 1>(fin, n, rowoff, dim, x0, fs, mask, lane);
 }
 
 template <int V> struct MapWord;
@@ -703,11 +662,8 @@ __device__ __forceinline__ void face_fix(const StepArgs &a, size_t rowoff, int x
     }
 }
 
-// mask != 0: the threads in `mask` run this together (rows of consecutive
-// threads), and x-shifted neighbours come from the neighbouring lanes
 template <class S, int MODE, int V, bool INTERIOR>
-__device__ __forceinline__ void pull_vector(const StepArgs &a, int xv, int y, int z, double &red_m, double &red_e,
-                                            unsigned mask = 0)
+__device__ __forceinline__ void pull_vector(const StepArgs &a, int xv, int y, int z, double &red_m, double &red_e)
 {
     const int dim = a.dim;
     const int x0 = xv * V;
@@ -717,8 +673,7 @@ __device__ __forceinline__ void pull_vector(const StepArgs &a, int xv, int y, in
     if (!INTERIOR) mw = __ldg(reinterpret_cast<const typename MapWord<V>::type *>(a.map + site0));
     const S *__restrict__ fin = static_cast<const S *>(a.fin);
     S fs[Q][V];
-    if (LBM_HALO_SHFL && mask) gather_all_lanes<S, V, 0>(fin, a.n, rowoff, dim, x0, fs, mask, (int)(threadIdx.x & 31));
-    else gather_all<S, V, 0>(fin, a.n, rowoff, dim, x0, fs);
+    gather_all<S, V, 0>(fin, a.n, rowoff, dim, x0, fs);
     update_vector<S, MODE, V, INTERIOR>(fs, mw, a, y, z, x0, site0, red_m, red_e);
     if (INTERIOR && MODE != MODE_REDUCE) {
         // the walls (x = 0, dim-1) hold values nobody reads; the faces bounce back
@@ -802,9 +757,7 @@ __global__ void __launch_bounds__(LBM_PULL_MAXT, min_blocks<S, VB>()) pull_kerne
     double red_m = 0.0, red_e = 0.0;
     const unsigned nrows = ROWS == ROWS_INTERIOR ? (unsigned)(a.dim - 4) * (unsigned)(a.dim - 4)
                                                  : 4u * (unsigned)(a.dim - 3);
-    const bool active = g < nrows * (unsigned)a.nvx;
-    const unsigned mask = __ballot_sync(0xffffffffu, active);
-    if (active) {
+    if (g < nrows * (unsigned)a.nvx) {
         const int dim = a.dim;
         const unsigned row = g / (unsigned)a.nvx;
         const int xv = (int)(g - row * (unsigned)a.nvx);
@@ -815,7 +768,7 @@ __global__ void __launch_bounds__(LBM_PULL_MAXT, min_blocks<S, VB>()) pull_kerne
         } else {
             decode_face_row(dim, row, y, z);
         }
-        pull_vector<S, MODE, V, ROWS == ROWS_INTERIOR>(a, xv, y, z, red_m, red_e, mask);
+        pull_vector<S, MODE, V, ROWS == ROWS_INTERIOR>(a, xv, y, z, red_m, red_e);
     }
     if (MODE == MODE_REDUCE) block_reduce_write(red_m, red_e, a.partials + 2 * (size_t)a.partial_base);
 }
