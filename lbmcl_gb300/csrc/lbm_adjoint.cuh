@@ -126,6 +126,18 @@ __device__ __forceinline__ void adjoint_moving(const A (&g)[Q], A (&b)[Q], A lid
 //   G  = sum_c w_c sum_pairs e_i (3 d + 9 a s) - 3 u SB,  SB = sum_c w_c sum s
 //   a_(+-) = (1 - omega) b_(+-) + omega (B0 - G.u) +- omega G.e_i
 //   dJ/domega += rho B0 - sum_i b_i g_i
+// e_i . u as a signed sum of the non-zero terms (chosen at compile time: no
+// multiplications by the 0 / +-1 components)
+template <class A> __device__ __forceinline__ A proj_sum(int i, A ux, A uy, A uz)
+{
+    A s = 0;
+    bool first = true;
+    if (ex_of(i)) { s = ex_of(i) > 0 ? ux : -ux; first = false; }
+    if (ey_of(i)) { s = first ? (ey_of(i) > 0 ? uy : -uy) : (ey_of(i) > 0 ? s + uy : s - uy); first = false; }
+    if (ez_of(i)) s = first ? (ez_of(i) > 0 ? uz : -uz) : (ez_of(i) > 0 ? s + uz : s - uz);
+    return s;
+}
+
 template <class A>
 __device__ __forceinline__ A adjoint_fluid_core(A (&b)[Q], A ux, A uy, A uz, A omega)
 {
@@ -139,7 +151,7 @@ __device__ __forceinline__ A adjoint_fluid_core(A (&b)[Q], A ux, A uy, A uz, A o
     for (int k = 0; k < 9; ++k) {
         const int i = P[k][0], j = P[k][1];
         const int c = wclass_of(i);
-        const A aa = (A)ex_of(i) * ux + (A)ey_of(i) * uy + (A)ez_of(i) * uz;
+        const A aa = proj_sum<A>(i, ux, uy, uz);
         const A sm = b[i] + b[j], df = b[i] - b[j];
         B[c] += sm * (c0 + (A)4.5 * aa * aa) + (A)3 * aa * df;
         SB[c] += sm;
@@ -453,6 +465,13 @@ __global__ void __launch_bounds__(256, sizeof(A) == 8 ? 1 : LBM_ADJ_MINB) adjoin
 // ---------------------------------------------------------------------------
 constexpr int ADJ2_EX = 32, ADJ2_EY = 8;                    // block = ext tile
 constexpr int ADJ2_TX = ADJ2_EX - 2, ADJ2_TY = ADJ2_EY - 2;  // owned tile
+// The stored-point variant (MACRO) needs 64 registers, so it runs taller
+// tiles, 32 x 16 (512 threads, two blocks per SM): the ring step A computes
+// for its neighbours is then 18% of its sites instead of 30%
+#ifndef LBM_ADJ2M_EY
+#define LBM_ADJ2M_EY 16
+#endif
+template <bool MACRO> __host__ __device__ constexpr int adj2_ey() { return MACRO ? LBM_ADJ2M_EY : ADJ2_EY; }
 __host__ __device__ constexpr bool adj2_in_regs(int i) { return i == 0 || i == 5 || i == 6; }
 __host__ __device__ constexpr int adj2_depth(int i)
 {
@@ -471,6 +490,10 @@ __host__ __device__ constexpr Adj2Layout adj2_layout()
 }
 constexpr int ADJ2_SLOTS = adj2_layout().base[Q];
 constexpr size_t ADJ2_SMEM = (size_t)ADJ2_SLOTS * ADJ2_EX * ADJ2_EY * sizeof(float);
+template <bool MACRO> __host__ __device__ constexpr size_t adj2_smem_bytes()
+{
+    return (size_t)ADJ2_SLOTS * ADJ2_EX * adj2_ey<MACRO>() * sizeof(float);
+}
 static_assert(ADJ2_SLOTS == 48, "plane slots of the two-step adjoint");
 // the largest dim whose 19 dim^3 element offsets fit 32 bits
 constexpr int ADJ2_MAX_DIM = 609;
@@ -501,7 +524,7 @@ struct Adj2Args {
 // registers: 64 registers without spills; four blocks measured 2% faster
 // than three at 256^3 FP16)
 #ifndef LBM_ADJ2M_MINB
-#define LBM_ADJ2M_MINB 4
+#define LBM_ADJ2M_MINB (32 / LBM_ADJ2M_EY)
 #endif
 
 // a_k(s) of one site of step A or B: b = the reverse-streamed adjoint, v =
@@ -531,11 +554,12 @@ __device__ __forceinline__ void adjoint_pull(const S *__restrict__ fwd, const un
 // MACRO = true: fwd_a / fwd_b hold the three MODE_STEP_ADJ planes (float) of
 // Q_k / Q_{k-1} instead of the states, and no tau term is formed.
 template <class S, bool MACRO>
-__global__ void __launch_bounds__(ADJ2_EX * ADJ2_EY, MACRO ? LBM_ADJ2M_MINB : LBM_ADJ2_MINB)
+__global__ void __launch_bounds__(ADJ2_EX * adj2_ey<MACRO>(), MACRO ? LBM_ADJ2M_MINB : LBM_ADJ2_MINB)
     adjoint2_kernel(Adj2Args a)
 {
-    extern __shared__ float adj2_smem[];  // [ADJ2_SLOTS][ADJ2_EY][ADJ2_EX]
-    constexpr int PL = ADJ2_EX * ADJ2_EY;
+    extern __shared__ float adj2_smem[];  // [ADJ2_SLOTS][EY][ADJ2_EX]
+    constexpr int EY = adj2_ey<MACRO>(), TY = EY - 2;
+    constexpr int PL = ADJ2_EX * EY;
     constexpr Adj2Layout LAY = adj2_layout();
     const int dim = a.dim;
     const unsigned plane = (unsigned)dim * (unsigned)dim;
@@ -544,15 +568,15 @@ __global__ void __launch_bounds__(ADJ2_EX * ADJ2_EY, MACRO ? LBM_ADJ2M_MINB : LB
     const int tx = t % a.ntx;
     t /= a.ntx;
     const int ty = t % a.nty, tz = t / a.nty;
-    const int xi0 = 1 + tx * ADJ2_TX, yi0 = 1 + ty * ADJ2_TY, zi0 = 1 + tz * a.zc;
+    const int xi0 = 1 + tx * ADJ2_TX, yi0 = 1 + ty * TY, zi0 = 1 + tz * a.zc;
     const int zi1 = min(zi0 + a.zc, dim - 1);  // owned planes [zi0, zi1)
     const int x = xi0 - 1 + lx, y = yi0 - 1 + ly;
     const bool in_dom = x < dim && y < dim;
-    const bool owned = lx >= 1 && lx <= ADJ2_TX && ly >= 1 && ly <= ADJ2_TY && x <= dim - 2 && y <= dim - 2;
+    const bool owned = lx >= 1 && lx <= ADJ2_TX && ly >= 1 && ly <= TY && x <= dim - 2 && y <= dim - 2;
     // block-uniform: every site of the ext tile / owned tile in x, y is FLUID
     // on the planes [2, dim-3]
-    const bool ext_fluid = xi0 - 1 >= 2 && xi0 + ADJ2_EX - 2 <= dim - 3 && yi0 - 1 >= 2 && yi0 + ADJ2_EY - 2 <= dim - 3;
-    const bool own_fluid = xi0 >= 2 && xi0 + ADJ2_TX - 1 <= dim - 3 && yi0 >= 2 && yi0 + ADJ2_TY - 1 <= dim - 3;
+    const bool ext_fluid = xi0 - 1 >= 2 && xi0 + ADJ2_EX - 2 <= dim - 3 && yi0 - 1 >= 2 && yi0 + EY - 2 <= dim - 3;
+    const bool own_fluid = xi0 >= 2 && xi0 + ADJ2_TX - 1 <= dim - 3 && yi0 >= 2 && yi0 + TY - 1 <= dim - 3;
     const S *fwd_a = static_cast<const S *>(a.fwd_a);
     const S *fwd_b = static_cast<const S *>(a.fwd_b);
     const float *lid = static_cast<const float *>(a.lid);
@@ -657,132 +681,6 @@ __global__ void __launch_bounds__(ADJ2_EX * ADJ2_EY, MACRO ? LBM_ADJ2M_MINB : LB
     // one MOVING site per column, in one chunk: a single writer per column
     if (owned && zi0 <= dim - 2 && dim - 2 < zi1) a.grad_lid[col] += (double)dl;
     if constexpr (!MACRO) block_reduce_add((double)dw, a.tau_acc);
-}
-
-// ---------------------------------------------------------------------------
-// The stored-point two-step adjoint with the next plane's step-A loads in
-// flight during the current plane's work: a thread loads the reverse-streamed
-// a_{k+1} (19 values), the linearisation point (3) and the map byte of plane
-// p + 1 into registers before it computes plane p, so that the load round
-// trip overlaps the two steps' arithmetic and the plane barrier instead of
-// preceding them.  Without the pulled populations a site's step-A inputs are
-// 22 values, which leaves room for a second set at two blocks per SM.  Same
-// tiles, plane slots and arithmetic as adjoint2_kernel<S, true>.
-// ---------------------------------------------------------------------------
-#ifndef LBM_ADJ2P_MINB
-#define LBM_ADJ2P_MINB 3
-#endif
-
-template <class S>
-__global__ void __launch_bounds__(ADJ2_EX * ADJ2_EY, LBM_ADJ2P_MINB) adjoint2p_kernel(Adj2Args a)
-{
-    extern __shared__ float adj2_smem[];  // [ADJ2_SLOTS][ADJ2_EY][ADJ2_EX]
-    constexpr int PL = ADJ2_EX * ADJ2_EY;
-    constexpr Adj2Layout LAY = adj2_layout();
-    const int dim = a.dim;
-    const unsigned plane = (unsigned)dim * (unsigned)dim;
-    const int lx = (int)threadIdx.x % ADJ2_EX, ly = (int)threadIdx.x / ADJ2_EX;
-    int t = (int)blockIdx.x;
-    const int tx = t % a.ntx;
-    t /= a.ntx;
-    const int ty = t % a.nty, tz = t / a.nty;
-    const int xi0 = 1 + tx * ADJ2_TX, yi0 = 1 + ty * ADJ2_TY, zi0 = 1 + tz * a.zc;
-    const int zi1 = min(zi0 + a.zc, dim - 1);  // owned planes [zi0, zi1)
-    const int x = xi0 - 1 + lx, y = yi0 - 1 + ly;
-    const bool in_dom = x < dim && y < dim;
-    const bool owned = lx >= 1 && lx <= ADJ2_TX && ly >= 1 && ly <= ADJ2_TY && x <= dim - 2 && y <= dim - 2;
-    const bool ext_fluid = xi0 - 1 >= 2 && xi0 + ADJ2_EX - 2 <= dim - 3 && yi0 - 1 >= 2 && yi0 + ADJ2_EY - 2 <= dim - 3;
-    const bool own_fluid = xi0 >= 2 && xi0 + ADJ2_TX - 1 <= dim - 3 && yi0 >= 2 && yi0 + ADJ2_TY - 1 <= dim - 3;
-    const float *pa = static_cast<const float *>(a.fwd_a);
-    const float *pb = static_cast<const float *>(a.fwd_b);
-    const float *lid = static_cast<const float *>(a.lid);
-    const float omega = a.omega;
-    float dl = 0.f;
-    const unsigned col = (unsigned)y * (unsigned)dim + (unsigned)x;
-    const float lidv = lid[in_dom ? col : 0];
-    float r0_prev = 0.f, r5_prev1 = 0.f, r5_prev2 = 0.f;
-
-    // step-A inputs of the next plane
-    float nb[Q], nm[3];
-    uint8_t nb8 = M_WALL;
-    auto fetch = [&](int p) {
-        const unsigned site = (unsigned)p * plane + col;
-        nb8 = M_WALL;
-        if (in_dom) nb8 = (ext_fluid && p >= 2 && p <= dim - 3) ? (uint8_t)0 : __ldg(a.map + site);
-        if (!(nb8 & M_WALL)) {
-#pragma unroll
-            for (int i = 0; i < Q; ++i) nb[i] = __ldg(a.ain + (site + a.off_up[i]));
-            nm[0] = __ldg(pa + site);
-            nm[1] = __ldg(pa + (site + a.off_own[1]));
-            nm[2] = __ldg(pa + (site + a.off_own[2]));
-        }
-    };
-    fetch(zi0 - 1);
-
-    for (int p = zi0 - 1; p <= zi1; ++p) {
-        float b[Q], r0, r5, r6;
-        const uint8_t b8a = nb8;
-        const float m0 = nm[0], m1 = nm[1], m2 = nm[2];
-#pragma unroll
-        for (int i = 0; i < Q; ++i) b[i] = nb[i];
-        if (p + 1 <= zi1) fetch(p + 1);
-        // ---- step A: a_k at (x, y, p) of the ext tile
-        if (b8a & M_WALL) {
-#pragma unroll
-            for (int i = 0; i < Q; ++i) b[i] = 0.f;
-        } else {
-            float l = 0.f;
-            adjoint_site_macro<float>(b, b8a, m0, m1, m2, (b8a & M_FRONT) ? lidv : 0.f, omega, l);
-            if (owned && p >= zi0 && p < zi1) dl += l;
-        }
-        {
-            const int m2s = p & 1, m3s = p % 3, m4s = p & 3;
-#pragma unroll
-            for (int i = 0; i < Q; ++i) {
-                if (adj2_in_regs(i)) continue;
-                const int slot = LAY.base[i] + (adj2_depth(i) == 2 ? m2s : (adj2_depth(i) == 3 ? m3s : m4s));
-                adj2_smem[slot * PL + threadIdx.x] = b[i];
-            }
-        }
-        r0 = b[0];
-        r5 = b[5];
-        r6 = b[6];
-        // ---- step B: a_{k-1} at (x, y, p - 1) of the owned tile
-        const int q = p - 1;
-        const bool do_b = owned && q >= zi0;
-        const unsigned site_b = (unsigned)q * plane + col;
-        float mb[3] = {0.f, 0.f, 0.f};
-        uint8_t b8b = 0;
-        if (do_b) {  // owned sites are never walls
-            b8b = (own_fluid && q >= 2 && q <= dim - 3) ? (uint8_t)0 : __ldg(a.map + site_b);
-            mb[0] = __ldg(pb + site_b);
-            mb[1] = __ldg(pb + (site_b + a.off_own[1]));
-            mb[2] = __ldg(pb + (site_b + a.off_own[2]));
-        }
-        __syncthreads();
-        if (do_b) {
-            const int m2s = p & 1, m3s = (p + 2) % 3, m4s = (p + 2) & 3;
-            float bb[Q];
-#pragma unroll
-            for (int i = 0; i < Q; ++i) {
-                if (adj2_in_regs(i)) continue;
-                const int slot = LAY.base[i] + (adj2_depth(i) == 2 ? m2s : (adj2_depth(i) == 3 ? m3s : m4s));
-                bb[i] = adj2_smem[slot * PL + (ly + ey_of(i)) * ADJ2_EX + (lx + ex_of(i))];
-            }
-            bb[0] = r0_prev;
-            bb[5] = r5_prev2;
-            bb[6] = r6;
-            float l = 0.f;
-            adjoint_site_macro<float>(bb, b8b, mb[0], mb[1], mb[2], (b8b & M_FRONT) ? lidv : 0.f, omega, l);
-            dl += l;
-#pragma unroll
-            for (int i = 0; i < Q; ++i) a.aout[site_b + a.off_own[i]] = bb[i];
-        }
-        r0_prev = r0;
-        r5_prev2 = r5_prev1;
-        r5_prev1 = r5;
-    }
-    if (owned && zi0 <= dim - 2 && dim - 2 < zi1) a.grad_lid[col] += (double)dl;
 }
 
 // Seed of the backward sweep: a_T = dJ/dR_T for the mid-plane loss

@@ -117,11 +117,13 @@ cudaError_t run_lid_init_grad(const lbm::AdjArgs &a, cudaStream_t s)
 // ---- two steps per launch (FP32 adjoint)
 constexpr int kAdj2Chunk = 24;  // z-planes per block (measured at 256^3: 16, 24, 32, 48 -> 24 best by 2%)
 
-unsigned adj2_grid(const lbm_t *h, int &ntx, int &nty)
+// blocks of the two-step launch (macro: the stored-point kernel's taller tiles)
+unsigned adj2_grid(const lbm_t *h, int &ntx, int &nty, bool macro)
 {
     const int m = h->dim - 2;
+    const int ty = (macro ? lbm::adj2_ey<true>() : lbm::adj2_ey<false>()) - 2;
     ntx = (m + lbm::ADJ2_TX - 1) / lbm::ADJ2_TX;
-    nty = (m + lbm::ADJ2_TY - 1) / lbm::ADJ2_TY;
+    nty = (m + ty - 1) / ty;
     const int ntz = (m + kAdj2Chunk - 1) / kAdj2Chunk;
     return (unsigned)ntx * (unsigned)nty * (unsigned)ntz;
 }
@@ -134,33 +136,24 @@ bool two_step(const lbm_t *h)
     if (adj64(h) || h->cfg.adjoint_steps == 1 || h->dim > lbm::ADJ2_MAX_DIM) return false;
     if (h->cfg.adjoint_steps == 2) return true;
     int ntx, nty;
-    return adj2_grid(h, ntx, nty) >= 2u * (unsigned)std::max(h->num_sms, 1);
+    return adj2_grid(h, ntx, nty, false) >= 2u * (unsigned)std::max(h->num_sms, 1);
 }
-
-// the stored-point sweep's two-step kernel: with the next plane's loads
-// prefetched (1, default) or without (0)
-#ifndef LBM_ADJ2_PREFETCH
-#define LBM_ADJ2_PREFETCH 1
-#endif
 
 template <class S, bool MACRO>
 cudaError_t run_adjoint2(const lbm::Adj2Args &a, unsigned grid, cudaStream_t s)
 {
-    if (MACRO && LBM_ADJ2_PREFETCH)
-        lbm::adjoint2p_kernel<S><<<grid, lbm::ADJ2_EX * lbm::ADJ2_EY, lbm::ADJ2_SMEM, s>>>(a);
-    else
-        lbm::adjoint2_kernel<S, MACRO><<<grid, lbm::ADJ2_EX * lbm::ADJ2_EY, lbm::ADJ2_SMEM, s>>>(a);
+    lbm::adjoint2_kernel<S, MACRO>
+        <<<grid, lbm::ADJ2_EX * lbm::adj2_ey<MACRO>(), lbm::adj2_smem_bytes<MACRO>(), s>>>(a);
     return cudaGetLastError();
 }
 
 template <class S>
 cudaError_t set_adjoint2_smem()
 {
-    const int bytes = (int)lbm::ADJ2_SMEM;
     const cudaFuncAttribute at = cudaFuncAttributeMaxDynamicSharedMemorySize;
-    cudaError_t e = cudaFuncSetAttribute(lbm::adjoint2_kernel<S, false>, at, bytes);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(lbm::adjoint2_kernel<S, true>, at, bytes);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(lbm::adjoint2p_kernel<S>, at, bytes);
+    cudaError_t e = cudaFuncSetAttribute(lbm::adjoint2_kernel<S, false>, at, (int)lbm::adj2_smem_bytes<false>());
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(lbm::adjoint2_kernel<S, true>, at, (int)lbm::adj2_smem_bytes<true>());
     return e;
 }
 
@@ -202,7 +195,7 @@ cudaError_t adjoint_two_steps(const lbm_t *h, const void *fwd_a, const void *fwd
         a.off_own[i] = (unsigned)base;
     }
     a.omega = (float)h->inv_tau;
-    const unsigned grid = adj2_grid(h, a.ntx, a.nty);
+    const unsigned grid = adj2_grid(h, a.ntx, a.nty, macro);
     switch (h->prec) {
     case LBM_FP32: return macro ? run_adjoint2<float, true>(a, grid, h->stream) : run_adjoint2<float, false>(a, grid, h->stream);
     case LBM_FP16:
@@ -607,7 +600,7 @@ int lbm_adjoint_backward(lbm_t *h, double dloss, double *grad_tau, double *grad_
     adj_grids(h, gi, gf);
     int ntx, nty;
     // tau partial slots: the one-step launch pair, or the two-step launch
-    const unsigned agrid = std::max(gi + gf, two_step(h) ? adj2_grid(h, ntx, nty) : 0u);
+    const unsigned agrid = std::max(gi + gf, two_step(h) ? adj2_grid(h, ntx, nty, false) : 0u);
     if (!s.adj[0]) {
         int rc = alloc_tracked(h, &s.adj[0], abytes);
         if (rc == LBM_OK) rc = alloc_tracked(h, &s.adj[1], abytes);

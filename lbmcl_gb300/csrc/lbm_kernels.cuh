@@ -22,11 +22,6 @@
 #include "lbm_device.cuh"
 #include "lbm_noise.cuh"
 
-// 16-bit storage: macro / linearisation-point stores of four sites at a time
-// (1) or of pairs (0)
-#ifndef LBM_QUAD_STORES
-#define LBM_QUAD_STORES 1
-#endif
 
 namespace lbm {
 
@@ -453,36 +448,6 @@ __device__ __forceinline__ void store_macro_pair(const StepArgs &a, size_t id, b
     }
 }
 
-// rho / u (MODE_STEP_MACRO) or the FLUID linearisation point (MODE_STEP_ADJ)
-// of four neighbouring FLUID sites (id a multiple of 4, FP32 macro type):
-// the first pair's values held as floats (h: r0 r1 ux0 ux1 uy0 uy1 uz0 uz1),
-// one 16-byte store per field when all four store (`all`), else per site
-template <int MODE>
-__device__ __forceinline__ void store_macro_quad(const StepArgs &a, size_t id, bool all, const float (&h)[8],
-                                                 bool s0, bool s1, const SiteOut &o2, const SiteOut &o3, bool s2,
-                                                 bool s3)
-{
-    float *u = static_cast<float *>(a.u);
-    float *rho = static_cast<float *>(a.rho);
-    if (all) {
-        if (MODE == MODE_STEP_MACRO)
-            *reinterpret_cast<float4 *>(rho + id) = make_float4(h[0], h[1], (float)o2.r, (float)o3.r);
-        *reinterpret_cast<float4 *>(u + id) = make_float4(h[2], h[3], (float)o2.ux, (float)o3.ux);
-        *reinterpret_cast<float4 *>(u + a.n + id) = make_float4(h[4], h[5], (float)o2.uy, (float)o3.uy);
-        *reinterpret_cast<float4 *>(u + 2 * a.n + id) = make_float4(h[6], h[7], (float)o2.uz, (float)o3.uz);
-        return;
-    }
-#pragma unroll
-    for (int j = 0; j < 2; ++j) {
-        if (!(j ? s1 : s0)) continue;
-        if (MODE == MODE_STEP_MACRO) rho[id + j] = h[j];
-        u[id + j] = h[2 + j];
-        u[a.n + id + j] = h[4 + j];
-        u[2 * a.n + id + j] = h[6 + j];
-    }
-    store_macro_pair<float, MODE>(a, id + 2, s2, s3, o2, o3);
-}
-
 __device__ __forceinline__ void accumulate(const SiteOut &o, double &m, double &e)
 {
     m += o.r;
@@ -579,8 +544,6 @@ __device__ __forceinline__ void update_vector(S (&fs)[Q][V], typename MapWord<V>
         if (FLUID_ONLY || mw == 0) {
             // all V sites FLUID (the bulk of the lattice): no per-site branches,
             // two sites per step so the output converts as packed pairs
-            float hq[8];
-            bool qf0 = false, qf1 = false;
 #pragma unroll
             for (int k = 0; k < V; k += 2) {
                 float D0[Q], D1[Q];
@@ -600,26 +563,8 @@ __device__ __forceinline__ void update_vector(S (&fs)[Q][V], typename MapWord<V>
                 const bool f0 = !FLUID_ONLY || (unsigned)(x0 + k - 2) <= (unsigned)(dim - 5);
                 const bool f1 = !FLUID_ONLY || (unsigned)(x0 + k - 1) <= (unsigned)(dim - 5);
                 bad |= (f0 && o0.bad) || (f1 && o1.bad);
-                if constexpr ((MODE == MODE_STEP_MACRO || MODE == MODE_STEP_ADJ) && V % 4 == 0 && LBM_QUAD_STORES) {
-                    // four sites per 16-byte store: the first pair waits in
-                    // registers for the second
-                    if ((k & 2) == 0) {
-                        hq[0] = (float)o0.r;
-                        hq[1] = (float)o1.r;
-                        hq[2] = (float)o0.ux;
-                        hq[3] = (float)o1.ux;
-                        hq[4] = (float)o0.uy;
-                        hq[5] = (float)o1.uy;
-                        hq[6] = (float)o0.uz;
-                        hq[7] = (float)o1.uz;
-                        qf0 = f0;
-                        qf1 = f1;
-                    } else {
-                        store_macro_quad<MODE>(a, site0 + k - 2, qf0 && qf1 && f0 && f1, hq, qf0, qf1, o0, o1, f0, f1);
-                    }
-                } else if constexpr (MODE == MODE_STEP_MACRO || MODE == MODE_STEP_ADJ) {
+                if constexpr (MODE == MODE_STEP_MACRO || MODE == MODE_STEP_ADJ)
                     store_macro_pair<C, MODE>(a, site0 + k, f0, f1, o0, o1);
-                }
                 if (MODE == MODE_REDUCE) {
                     if (f0) accumulate(o0, red_m, red_e);
                     if (f1) accumulate(o1, red_m, red_e);
