@@ -139,11 +139,20 @@ bool two_step(const lbm_t *h)
     return adj2_grid(h, ntx, nty, false) >= 2u * (unsigned)std::max(h->num_sms, 1);
 }
 
+// the stored-point sweep's two-step kernel: step-A inputs staged by cp.async
+// (1, default) or loaded directly (0)
+#ifndef LBM_ADJ2_ASYNC
+#define LBM_ADJ2_ASYNC 1
+#endif
+
 template <class S, bool MACRO>
 cudaError_t run_adjoint2(const lbm::Adj2Args &a, unsigned grid, cudaStream_t s)
 {
-    lbm::adjoint2_kernel<S, MACRO>
-        <<<grid, lbm::ADJ2_EX * lbm::adj2_ey<MACRO>(), lbm::adj2_smem_bytes<MACRO>(), s>>>(a);
+    if (MACRO && LBM_ADJ2_ASYNC && lbm::adj2_ey<MACRO>() == lbm::ADJ2_EY)
+        lbm::adjoint2a_kernel<S><<<grid, lbm::ADJ2_EX * lbm::ADJ2_EY, lbm::ADJ2A_SMEM, s>>>(a);
+    else
+        lbm::adjoint2_kernel<S, MACRO>
+            <<<grid, lbm::ADJ2_EX * lbm::adj2_ey<MACRO>(), lbm::adj2_smem_bytes<MACRO>(), s>>>(a);
     return cudaGetLastError();
 }
 
@@ -154,6 +163,7 @@ cudaError_t set_adjoint2_smem()
     cudaError_t e = cudaFuncSetAttribute(lbm::adjoint2_kernel<S, false>, at, (int)lbm::adj2_smem_bytes<false>());
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(lbm::adjoint2_kernel<S, true>, at, (int)lbm::adj2_smem_bytes<true>());
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(lbm::adjoint2a_kernel<S>, at, (int)lbm::ADJ2A_SMEM);
     return e;
 }
 
