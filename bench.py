@@ -394,6 +394,8 @@ def main():
     ap.add_argument("--no-config2", action="store_true", help="skip the 256^3 FP32 / FP64 leg")
     ap.add_argument("--repeats", type=int, default=5,
                     help="timed windows of --steps iterations for the headline mode (median reported)")
+    ap.add_argument("--min-window", type=float, default=1.0,
+                    help="seconds of headline windows at least (clock samples under load)")
     ap.add_argument("--modes", default="fp16,bf16,fp32,fp64")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -429,7 +431,7 @@ def main():
         k = args.steps if head_mode else (max(10, args.steps // 5) if m != "fp64" else max(5, args.steps // 50))
         ms, wins = time_mode(capi, m, k, args.warmup if m != "fp64" else 3, device, barrier,
                              sampler if head_mode else None, repeats=args.repeats if head_mode else 1,
-                             min_window_s=1.0 if head_mode else 0.0)
+                             min_window_s=args.min_window if head_mode else 0.0)
         ms = slowest_rank_ms(ms, ws, f"cuda:{device}")
         mlups = wet / (ms * 1e3)
         gbs = wet * BYTES_PER_SITE[m] / (ms * 1e-3) / 1e9

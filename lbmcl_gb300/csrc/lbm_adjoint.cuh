@@ -683,156 +683,6 @@ __global__ void __launch_bounds__(ADJ2_EX * adj2_ey<MACRO>(), MACRO ? LBM_ADJ2M_
     if constexpr (!MACRO) block_reduce_add((double)dw, a.tau_acc);
 }
 
-// ---------------------------------------------------------------------------
-// The stored-point two-step adjoint with its step-A inputs staged by
-// cp.async: a thread copies the reverse-streamed a_{k+1} (19 values) and the
-// linearisation point (3) of its site on plane p + 1 from global into its own
-// 22 shared-memory slots while it computes plane p, and reads them back at the
-// start of plane p + 1.  The copies need no registers and are issued before
-// the plane's arithmetic and barrier, so their round trip overlaps them; a
-// thread reads only its own slots (one stage suffices: it takes plane p's
-// values before issuing plane p + 1's copies, and waits only for its own
-// copies).  Shared memory: the 48 plane slots of a_k plus 22 x 256 staging
-// floats (70.5 KB, three blocks per SM).  Same tiles and arithmetic as
-// adjoint2_kernel<S, true>.
-// ---------------------------------------------------------------------------
-constexpr int ADJ2A_STAGE = Q + 3;
-constexpr size_t ADJ2A_SMEM = ADJ2_SMEM + (size_t)ADJ2A_STAGE * ADJ2_EX * ADJ2_EY * sizeof(float);
-#ifndef LBM_ADJ2A_MINB
-#define LBM_ADJ2A_MINB 3
-#endif
-
-__device__ __forceinline__ void cp_async4(float *dst, const float *src)
-{
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
-                 : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
-
-template <class S>
-__global__ void __launch_bounds__(ADJ2_EX * ADJ2_EY, LBM_ADJ2A_MINB) adjoint2a_kernel(Adj2Args a)
-{
-    extern __shared__ float adj2_smem[];  // [ADJ2_SLOTS][EY][EX], then [ADJ2A_STAGE][EY][EX]
-    constexpr int PL = ADJ2_EX * ADJ2_EY;
-    constexpr Adj2Layout LAY = adj2_layout();
-    float *stage = adj2_smem + (size_t)ADJ2_SLOTS * PL;
-    const int dim = a.dim;
-    const unsigned plane = (unsigned)dim * (unsigned)dim;
-    const int lx = (int)threadIdx.x % ADJ2_EX, ly = (int)threadIdx.x / ADJ2_EX;
-    int t = (int)blockIdx.x;
-    const int tx = t % a.ntx;
-    t /= a.ntx;
-    const int ty = t % a.nty, tz = t / a.nty;
-    const int xi0 = 1 + tx * ADJ2_TX, yi0 = 1 + ty * ADJ2_TY, zi0 = 1 + tz * a.zc;
-    const int zi1 = min(zi0 + a.zc, dim - 1);  // owned planes [zi0, zi1)
-    const int x = xi0 - 1 + lx, y = yi0 - 1 + ly;
-    const bool in_dom = x < dim && y < dim;
-    const bool owned = lx >= 1 && lx <= ADJ2_TX && ly >= 1 && ly <= ADJ2_TY && x <= dim - 2 && y <= dim - 2;
-    const bool ext_fluid = xi0 - 1 >= 2 && xi0 + ADJ2_EX - 2 <= dim - 3 && yi0 - 1 >= 2 && yi0 + ADJ2_EY - 2 <= dim - 3;
-    const bool own_fluid = xi0 >= 2 && xi0 + ADJ2_TX - 1 <= dim - 3 && yi0 >= 2 && yi0 + ADJ2_TY - 1 <= dim - 3;
-    const float *pa = static_cast<const float *>(a.fwd_a);
-    const float *pb = static_cast<const float *>(a.fwd_b);
-    const float *lid = static_cast<const float *>(a.lid);
-    const float omega = a.omega;
-    float dl = 0.f;
-    const unsigned col = (unsigned)y * (unsigned)dim + (unsigned)x;
-    const float lidv = lid[in_dom ? col : 0];
-    float r0_prev = 0.f, r5_prev1 = 0.f, r5_prev2 = 0.f;
-    float *mine = stage + threadIdx.x;  // this thread's slots, stride PL
-
-    // the map byte of a plane (walls need no inputs), and the copies of a
-    // non-wall site's step-A inputs into this thread's slots
-    auto map_byte = [&](int p) -> uint8_t {
-        if (!in_dom) return M_WALL;
-        return (ext_fluid && p >= 2 && p <= dim - 3) ? (uint8_t)0 : __ldg(a.map + (unsigned)p * plane + col);
-    };
-    auto issue = [&](int p, uint8_t b8) {
-        if (!(b8 & M_WALL)) {
-            const unsigned site = (unsigned)p * plane + col;
-#pragma unroll
-            for (int i = 0; i < Q; ++i) cp_async4(mine + i * PL, a.ain + (site + a.off_up[i]));
-            cp_async4(mine + Q * PL, pa + site);
-            cp_async4(mine + (Q + 1) * PL, pa + (site + a.off_own[1]));
-            cp_async4(mine + (Q + 2) * PL, pa + (site + a.off_own[2]));
-        }
-        cp_async_commit();
-    };
-    uint8_t nb8 = map_byte(zi0 - 1);
-    issue(zi0 - 1, nb8);
-
-    for (int p = zi0 - 1; p <= zi1; ++p) {
-        float b[Q], m[3], r0, r5, r6;
-        const uint8_t b8a = nb8;
-        cp_async_wait_all();
-#pragma unroll
-        for (int i = 0; i < Q; ++i) b[i] = mine[i * PL];
-#pragma unroll
-        for (int c = 0; c < 3; ++c) m[c] = mine[(Q + c) * PL];
-        if (p + 1 <= zi1) {
-            nb8 = map_byte(p + 1);
-            issue(p + 1, nb8);
-        }
-        // ---- step A: a_k at (x, y, p) of the ext tile
-        if (b8a & M_WALL) {
-#pragma unroll
-            for (int i = 0; i < Q; ++i) b[i] = 0.f;
-        } else {
-            float l = 0.f;
-            adjoint_site_macro<float>(b, b8a, m[0], m[1], m[2], (b8a & M_FRONT) ? lidv : 0.f, omega, l);
-            if (owned && p >= zi0 && p < zi1) dl += l;
-        }
-        {
-            const int m2s = p & 1, m3s = p % 3, m4s = p & 3;
-#pragma unroll
-            for (int i = 0; i < Q; ++i) {
-                if (adj2_in_regs(i)) continue;
-                const int slot = LAY.base[i] + (adj2_depth(i) == 2 ? m2s : (adj2_depth(i) == 3 ? m3s : m4s));
-                adj2_smem[slot * PL + threadIdx.x] = b[i];
-            }
-        }
-        r0 = b[0];
-        r5 = b[5];
-        r6 = b[6];
-        // ---- step B: a_{k-1} at (x, y, p - 1) of the owned tile
-        const int q = p - 1;
-        const bool do_b = owned && q >= zi0;
-        const unsigned site_b = (unsigned)q * plane + col;
-        float mb[3] = {0.f, 0.f, 0.f};
-        uint8_t b8b = 0;
-        if (do_b) {  // owned sites are never walls
-            b8b = (own_fluid && q >= 2 && q <= dim - 3) ? (uint8_t)0 : __ldg(a.map + site_b);
-            mb[0] = __ldg(pb + site_b);
-            mb[1] = __ldg(pb + (site_b + a.off_own[1]));
-            mb[2] = __ldg(pb + (site_b + a.off_own[2]));
-        }
-        __syncthreads();
-        if (do_b) {
-            const int m2s = p & 1, m3s = (p + 2) % 3, m4s = (p + 2) & 3;
-            float bb[Q];
-#pragma unroll
-            for (int i = 0; i < Q; ++i) {
-                if (adj2_in_regs(i)) continue;
-                const int slot = LAY.base[i] + (adj2_depth(i) == 2 ? m2s : (adj2_depth(i) == 3 ? m3s : m4s));
-                bb[i] = adj2_smem[slot * PL + (ly + ey_of(i)) * ADJ2_EX + (lx + ex_of(i))];
-            }
-            bb[0] = r0_prev;
-            bb[5] = r5_prev2;
-            bb[6] = r6;
-            float l = 0.f;
-            adjoint_site_macro<float>(bb, b8b, mb[0], mb[1], mb[2], (b8b & M_FRONT) ? lidv : 0.f, omega, l);
-            dl += l;
-#pragma unroll
-            for (int i = 0; i < Q; ++i) a.aout[site_b + a.off_own[i]] = bb[i];
-        }
-        r0_prev = r0;
-        r5_prev2 = r5_prev1;
-        r5_prev1 = r5;
-    }
-    cp_async_wait_all();
-    if (owned && zi0 <= dim - 2 && dim - 2 < zi1) a.grad_lid[col] += (double)dl;
-}
-
 // Seed of the backward sweep: a_T = dJ/dR_T for the mid-plane loss
 //   J = (1/M) sum over the FLUID sites of plane y = plane_y of (u_x - target)^2,
 // dJ/dR_T(s, i) = (2/M) (u_x - target) (e_ix - u_x) / rho; zero elsewhere.

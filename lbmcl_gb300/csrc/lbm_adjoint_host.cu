@@ -115,7 +115,11 @@ cudaError_t run_lid_init_grad(const lbm::AdjArgs &a, cudaStream_t s)
 }
 
 // ---- two steps per launch (FP32 adjoint)
-constexpr int kAdj2Chunk = 24;  // z-planes per block (measured at 256^3: 16, 24, 32, 48 -> 24 best by 2%)
+// z-planes per block (measured at 256^3: 16, 24, 32, 48 -> 24 best by 2%)
+#ifndef LBM_ADJ2_CHUNK
+#define LBM_ADJ2_CHUNK 24
+#endif
+constexpr int kAdj2Chunk = LBM_ADJ2_CHUNK;
 
 // blocks of the two-step launch (macro: the stored-point kernel's taller tiles)
 unsigned adj2_grid(const lbm_t *h, int &ntx, int &nty, bool macro)
@@ -139,20 +143,11 @@ bool two_step(const lbm_t *h)
     return adj2_grid(h, ntx, nty, false) >= 2u * (unsigned)std::max(h->num_sms, 1);
 }
 
-// the stored-point sweep's two-step kernel: step-A inputs staged by cp.async
-// (1, default) or loaded directly (0)
-#ifndef LBM_ADJ2_ASYNC
-#define LBM_ADJ2_ASYNC 1
-#endif
-
 template <class S, bool MACRO>
 cudaError_t run_adjoint2(const lbm::Adj2Args &a, unsigned grid, cudaStream_t s)
 {
-    if (MACRO && LBM_ADJ2_ASYNC && lbm::adj2_ey<MACRO>() == lbm::ADJ2_EY)
-        lbm::adjoint2a_kernel<S><<<grid, lbm::ADJ2_EX * lbm::ADJ2_EY, lbm::ADJ2A_SMEM, s>>>(a);
-    else
-        lbm::adjoint2_kernel<S, MACRO>
-            <<<grid, lbm::ADJ2_EX * lbm::adj2_ey<MACRO>(), lbm::adj2_smem_bytes<MACRO>(), s>>>(a);
+    lbm::adjoint2_kernel<S, MACRO>
+        <<<grid, lbm::ADJ2_EX * lbm::adj2_ey<MACRO>(), lbm::adj2_smem_bytes<MACRO>(), s>>>(a);
     return cudaGetLastError();
 }
 
@@ -163,7 +158,6 @@ cudaError_t set_adjoint2_smem()
     cudaError_t e = cudaFuncSetAttribute(lbm::adjoint2_kernel<S, false>, at, (int)lbm::adj2_smem_bytes<false>());
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(lbm::adjoint2_kernel<S, true>, at, (int)lbm::adj2_smem_bytes<true>());
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(lbm::adjoint2a_kernel<S>, at, (int)lbm::ADJ2A_SMEM);
     return e;
 }
 
