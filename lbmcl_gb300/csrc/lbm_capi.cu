@@ -420,7 +420,9 @@ int lbm_init(lbm_t **out, const lbm_config *c)
     const size_t nvec = (size_t)(dim / V) * (size_t)(dim - 2) * (size_t)(dim - 2);
     unsigned block = c->block_threads > 0 ? (unsigned)(c->block_threads / 32 * 32) : 128u;
     if (block < 32) block = 32;
-    if (block > 256) block = 256;  // the pull kernel's launch bound
+    // the iteration kernels' launch bounds: 128 threads for 16-bit storage
+    const unsigned max_block = (prec == LBM_FP16 || prec == LBM_BF16) ? 128u : 256u;
+    if (block > max_block) block = max_block;
     // reduction partials: one pair per block of the widest launch (the AA
     // variant's FP32 kernels use 8-byte vectors, twice the threads)
     const int Vr = (c->kernel == LBM_KERNEL_AA && prec == LBM_FP32) ? V / 2 : V;

@@ -664,13 +664,18 @@ __device__ __forceinline__ void decode_face_row(int dim, unsigned br, int &y, in
     }
 }
 
-// Minimum resident 256-thread blocks per SM each direct kernel is compiled
-// for, i.e. its register cap 65536 / (256 n).  Measured at 512^3 on GB300:
-// 16-bit storage runs fastest at 128 registers (n = 2) with either vector
-// width, FP32 with 8-byte vectors at 85 (n = 3); FP64 is FP64-throughput bound
-// and left uncapped.
+// Launch bounds of the iteration kernels: the largest block each is compiled
+// for and the blocks of that size that must fit an SM, i.e. the register cap
+// 65536 / (threads n).  Measured at 512^3 on GB300: 16-bit storage runs
+// fastest at 128-thread blocks with three per SM (168 registers, no spills:
+// 84,448 MLUPS against 82,201 at 128 registers, which spill 88 bytes); FP32
+// with 8-byte vectors at 85 registers (256 x 3); FP64 is FP64-throughput bound
+// and left uncapped.  lbm_init clamps block_threads to max_threads.
 #ifndef LBM_MINB_16
-#define LBM_MINB_16 2
+#define LBM_MINB_16 3
+#endif
+#ifndef LBM_MAXT_16
+#define LBM_MAXT_16 128
 #endif
 #ifndef LBM_MINB_32_V16
 #define LBM_MINB_32_V16 2
@@ -687,15 +692,10 @@ template <class S, int VB> constexpr int min_blocks()
          : sizeof(S) == 4 ? (VB == 16 ? LBM_MINB_32_V16 : LBM_MINB_32_V8)
                           : LBM_MINB_64;
 }
-
-// largest block the pull / AA kernels are compiled for (the launcher clamps
-// block_threads to it)
-#ifndef LBM_PULL_MAXT
-#define LBM_PULL_MAXT 256
-#endif
+template <class S> constexpr int max_threads() { return sizeof(S) == 2 ? LBM_MAXT_16 : 256; }
 
 template <class S, int MODE, int VB, int ROWS>
-__global__ void __launch_bounds__(LBM_PULL_MAXT, min_blocks<S, VB>()) pull_kernel(StepArgs a)
+__global__ void __launch_bounds__(max_threads<S>(), min_blocks<S, VB>()) pull_kernel(StepArgs a)
 {
     constexpr int V = VB / (int)sizeof(S);
     const unsigned g = blockIdx.x * blockDim.x + threadIdx.x;
@@ -861,7 +861,7 @@ __device__ __forceinline__ void aa_vector(const StepArgs &a, bool active, int xv
 // the lattice, PHASE 0 = A-step, 1 = B-step.  Same row split and register
 // caps as pull_kernel.
 template <class S, int MODE, int VB, int ROWS, int PHASE>
-__global__ void __launch_bounds__(256, min_blocks<S, VB>()) aa_kernel(StepArgs a)
+__global__ void __launch_bounds__(max_threads<S>(), min_blocks<S, VB>()) aa_kernel(StepArgs a)
 {
     constexpr int V = VB / (int)sizeof(S);
     const unsigned g = blockIdx.x * blockDim.x + threadIdx.x;
