@@ -455,8 +455,9 @@ __global__ void __launch_bounds__(256, sizeof(A) == 8 ? 1 : LBM_ADJ_MINB) adjoin
 // last, pop 5 of the one before).  The other 16 live in shared memory for
 // the planes still to be read; with one barrier per plane the writer of plane
 // p+1 runs alongside the readers of plane p-1, so a population needs 2, 3 or
-// 4 plane slots for ez_i = +1, 0, -1 (48 slots, 49,152 bytes).  Three blocks
-// per SM at 80 registers measured faster than four at 64 (which spills).
+// 4 plane slots for ez_i = +1, 0, -1 (48 slots, 49,152 bytes).  The
+// full-state variant runs three blocks per SM at 80 registers (four at 64
+// spill); the stored-point variant four at 64.
 // Sums for tau and the lid gradient count a site once: step A's
 // contributions only on the block's own tile and planes.
 //
@@ -465,9 +466,9 @@ __global__ void __launch_bounds__(256, sizeof(A) == 8 ? 1 : LBM_ADJ_MINB) adjoin
 // ---------------------------------------------------------------------------
 constexpr int ADJ2_EX = 32, ADJ2_EY = 8;                    // block = ext tile
 constexpr int ADJ2_TX = ADJ2_EX - 2, ADJ2_TY = ADJ2_EY - 2;  // owned tile
-// The stored-point variant (MACRO) needs 64 registers, so it runs taller
-// tiles, 32 x 16 (512 threads, two blocks per SM): the ring step A computes
-// for its neighbours is then 18% of its sites instead of 30%
+// Tile height of the stored-point variant (MACRO): 8 rows; 16 rows (512
+// threads, two blocks per SM, a ring of 18% of the sites instead of 30%)
+// measured slower
 #ifndef LBM_ADJ2M_EY
 #define LBM_ADJ2M_EY 8
 #endif
