@@ -83,7 +83,9 @@ typedef struct lbm_config {
     int block_threads;         /* CUDA threads per block (from -w); 0 = tuned default       */
     uint64_t seed;             /* noise seed                                                */
     double noise_sigma;        /* std-dev of the N(0, sigma^2) noise added to every
-                                  population of FLUID sites after initialisation; 0 = none */
+                                  population of FLUID sites after initialisation; 0 = none;
+                                  sigma z is a float product (sigma rounded to float) for
+                                  FP32 and 16-bit storage, a double product for FP64     */
     const double *lid_profile; /* optional host array dim*dim: lid u_x of column (x,y)
                                   at lid_profile[x + y*dim]; NULL = velocity everywhere    */
     double tau;                /* > 0 overrides the viscosity                               */

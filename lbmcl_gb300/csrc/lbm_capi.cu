@@ -507,6 +507,7 @@ int lbm_init(lbm_t **out, const lbm_config *c)
         ia.n = n;
         ia.seed = c->seed;
         ia.noise_sigma = c->noise_sigma;
+        ia.noise_sigma_f = (float)c->noise_sigma;
         ia.in_place = aa ? 1 : 0;
         LBM_CUDA(cudaEventRecord(h->ev_first, h->stream));
         switch (prec) {

@@ -331,6 +331,7 @@ struct InitArgs {
     size_t n;
     uint64_t seed;
     double noise_sigma;
+    float noise_sigma_f;  // noise_sigma rounded to float (FP32 / 16-bit storage)
     int in_place;         // 1: the AA kernels' one lattice in A-form (f(s, i) = R_0(s, i));
                           // 0: P_{-1} of the two-lattice kernels
 };

@@ -1133,12 +1133,27 @@ __global__ void init_kernel(InitArgs a)
 
     S *f = static_cast<S *>(a.f);
     const Weights<C> W = make_weights<C>();
+    // With noise, noise_kernel writes every slot whose value belongs to a
+    // FLUID site (the slots streaming into it, or its own in A-form); this
+    // kernel writes the others.
+    const bool noisy = a.noise_sigma != 0.0;
+    if (x >= 3 && y >= 3 && z >= 3 && x <= dim - 4 && y <= dim - 4 && z <= dim - 4) {
+        // the site and all its neighbours are FLUID: the rest state
+        if (!noisy) {
+#pragma unroll
+            for (int i = 0; i < Q; ++i) {
+                if constexpr (is_dev16<S>()) f[(size_t)i * a.n + id] = Dev16<S>::from_f(0.0f);
+                else f[(size_t)i * a.n + id] = (S)W.w[wclass_of(i)];
+            }
+        }
+        return;
+    }
 #pragma unroll
     for (int i = 0; i < Q; ++i) {
         C val = qn;  // walls hold NaN (kernels.cl:312, 316)
         if (a.in_place) {
-            // A-form: the site's own R_0 slots, its initial equilibrium (the
-            // noise of FLUID sites is written by noise_kernel)
+            // A-form: the site's own R_0 slots, its initial equilibrium
+            if (noisy && b == 0) continue;
             if (!(b & M_WALL)) {
                 const C lv = (b & M_FRONT) ? lid_at<C>(a, x, y) : (C)0;
                 if constexpr (is_dev16<S>()) {
@@ -1155,11 +1170,11 @@ __global__ void init_kernel(InitArgs a)
         } else if (!(b & M_WALL)) {
             const int tx = x + ex_of(i), ty = y + ey_of(i), tz = z + ez_of(i);
             const uint8_t tb = pack_cell(dim, tx, ty, tz);
+            if (noisy && tb == 0) continue;
             if (!(tb & M_WALL)) {
                 const C lv = (tb & M_FRONT) ? lid_at<C>(a, tx, ty) : (C)0;
                 if constexpr (is_dev16<S>()) {
-                    // deviation of the equilibrium at rho = 1 (the noise of
-                    // FLUID targets is written by noise_kernel)
+                    // deviation of the equilibrium at rho = 1
                     float d = 0.0f;
                     if (tb & M_FRONT) {
                         const float eu = ex_of(i) > 0 ? (float)lv : (ex_of(i) < 0 ? -(float)lv : 0.0f);
@@ -1184,7 +1199,9 @@ __global__ void init_kernel(InitArgs a)
 // draws its ten sample pairs (populations 2m, 2m+1 <- pair m) and writes the
 // 19 slots (t - e_q, q) of P_{-1} that stream into t (in place: t's own
 // slots (t, q)), each slot having this one writer: the equilibrium at rest
-// (w_q; deviation 0) plus sigma z.
+// (w_q; deviation 0) plus sigma z.  sigma z is one single-precision product
+// (sigma rounded to float) for FP32 and 16-bit storage, a double product for
+// FP64 storage: GB300's FP64 pipe would otherwise bound this kernel.
 template <class S>
 __global__ void noise_kernel(InitArgs a)
 {
@@ -1205,15 +1222,16 @@ __global__ void noise_kernel(InitArgs a)
         for (int h = 0; h < 2; ++h) {
             const int q = 2 * p + h;
             if (q >= Q) break;
-            const double sz = __dmul_rn(a.noise_sigma, (double)(h ? z1 : z0));
+            const float zq = h ? z1 : z0;
             const ptrdiff_t sh = a.in_place ? 0
                                : (ptrdiff_t)ex_of(q) + (ptrdiff_t)ey_of(q) * dim + (ptrdiff_t)ez_of(q) * dim * dim;
             S *dst = f + (size_t)q * a.n + (size_t)((ptrdiff_t)t - sh);
             if constexpr (is_dev16<S>()) {
-                const float val = __fmul_rn((float)sz, Dev16<S>::scale);
-                *dst = Dev16<S>::from_f(val);
+                *dst = Dev16<S>::from_f(__fmul_rn(__fmul_rn(a.noise_sigma_f, zq), Dev16<S>::scale));
+            } else if constexpr (sizeof(C) == 4) {
+                *dst = (S)__fadd_rn(W.w[wclass_of(q)], __fmul_rn(a.noise_sigma_f, zq));
             } else {
-                *dst = (S)X<C>::add(W.w[wclass_of(q)], (C)sz);
+                *dst = (S)X<C>::add(W.w[wclass_of(q)], (C)__dmul_rn(a.noise_sigma, (double)zq));
             }
         }
     }

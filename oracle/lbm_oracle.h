@@ -53,7 +53,8 @@ typedef struct lbmo_params {
     double velocity;         /* lid u_x (VELOCITY), used when lid == NULL        */
     const double *lid;       /* optional per-column lid u_x, lid[x + y*dim]      */
     uint64_t seed;           /* noise seed                                        */
-    double noise_sigma;      /* 0: no noise                                       */
+    double noise_sigma;      /* 0: no noise; FP32 adds (float)sigma * z in float,
+                              * FP64 adds sigma * z in double                    */
     int threads;             /* OpenMP threads, 0: runtime default                */
 } lbmo_params;
 

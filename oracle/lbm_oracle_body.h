@@ -83,7 +83,11 @@ void SFX(lbmo_init)(const lbmo_params *p, REAL *f_stream, REAL *f_collide,
                 for (int i = 0; i < LBMO_Q; ++i) {
                     REAL fi = SFX(feq)(i, r0, ux, uy, uz, u2, w);
                     if (lbmo_is_wall(ct)) fi = qnan;
-                    if (noisy) fi = fi + (REAL)(p->noise_sigma * (double)z[i]);
+                    /* sigma z: a float product (sigma rounded to float) for
+                     * FP32, a double product for FP64 */
+                    if (noisy)
+                        fi = fi + (sizeof(REAL) == 4 ? (REAL)((float)p->noise_sigma * z[i])
+                                                     : (REAL)(p->noise_sigma * (double)z[i]));
                     f_collide[SFX(csoa)(id, i, sd)] = fi;
                     f_stream[SFX(csoa)(id, i, sd)] = fi;
                 }
