@@ -47,7 +47,10 @@ typedef enum lbm_status {
     LBM_ENOMEM = 2,    /* device allocation failed or exceeds max_device_bytes */
     LBM_ECUDA = 3,     /* a CUDA runtime call failed (no device, launch error) */
     LBM_ESTATE = 4,    /* call not valid in the handle's current state         */
-    LBM_EDIVERGED = 5  /* a site's density became <= 0 or NaN (lbm_sync)       */
+    LBM_EDIVERGED = 5, /* a site's density became <= 0 or NaN (lbm_sync)       */
+    LBM_ETIMEOUT = 6   /* a kernel's bounded wait expired (staged iteration
+                          kernel, two-step adjoint): the handle's results are
+                          not valid; the flag stays set on the handle        */
 } lbm_status;
 
 /* Population storage.  FP32/FP64 reproduce the reference's float / double

@@ -20,7 +20,7 @@ FP32, FP64, FP16, BF16 = 0, 1, 2, 3
 PRECISIONS = {"fp32": FP32, "fp64": FP64, "fp16": FP16, "bf16": BF16}
 KERNELS = {"auto": 0, "direct": 1, "staged": 2, "narrow": 3, "aa": 4}
 DUMP_F, DUMP_RHO, DUMP_U, DUMP_MAP, DUMP_MAP_U8, DUMP_F_RAW = 0, 1, 2, 3, 4, 5
-OK, EINVAL, ENOMEM, ECUDA, ESTATE, EDIVERGED = 0, 1, 2, 3, 4, 5
+OK, EINVAL, ENOMEM, ECUDA, ESTATE, EDIVERGED, ETIMEOUT = 0, 1, 2, 3, 4, 5, 6
 Q = 19
 
 

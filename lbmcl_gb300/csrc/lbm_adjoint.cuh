@@ -451,13 +451,12 @@ __global__ void __launch_bounds__(256, sizeof(A) == 8 ? 1 : LBM_ADJ_MINB) adjoin
 //
 // Step B at plane q reads population i of a_k at plane q + ez_i, x + ex_i,
 // y + ey_i.  Populations 0, 5 and 6 have no x, y offset: the same thread
-// computed them, so they stay in registers (pop 6 of this plane, pop 0 of the
-// last, pop 5 of the one before).  The other 16 live in shared memory for
-// the planes still to be read; with one barrier per plane the writer of plane
-// p+1 runs alongside the readers of plane p-1, so a population needs 2, 3 or
-// 4 plane slots for ez_i = +1, 0, -1 (48 slots, 49,152 bytes).  The
-// full-state variant runs three blocks per SM at 80 registers (four at 64
-// spill); the stored-point variant four at 64.
+// computed them, so they stay in registers, a short history per plane.  The
+// other 16 live in shared memory for the planes still to be read: with step
+// B one plane behind and one barrier per plane, the writer of plane p+1 runs
+// alongside the readers of plane p-1, so a population needs 2, 3 or 4 plane
+// slots for ez_i = +1, 0, -1 (48 slots, 48 KB); with step B two planes
+// behind (ADJ2_LAG) 3, 4 or 5 (64 slots, 64 KB).
 // Sums for tau and the lid gradient count a site once: step A's
 // contributions only on the block's own tile and planes.
 //
@@ -473,10 +472,20 @@ constexpr int ADJ2_TX = ADJ2_EX - 2, ADJ2_TY = ADJ2_EY - 2;  // owned tile
 #define LBM_ADJ2M_EY 8
 #endif
 template <bool MACRO> __host__ __device__ constexpr int adj2_ey() { return MACRO ? LBM_ADJ2M_EY : ADJ2_EY; }
+// Planes step B runs behind step A: 1 = one block barrier per plane between
+// them; 2 = an mbarrier whose arrival (after step A of plane p) and wait
+// (after step B of plane p - 2) enclose step B's work, so a block's warps
+// drift by up to one plane instead of meeting at every barrier; each
+// population then needs one more plane slot.
+#ifndef LBM_ADJ2_LAG
+#define LBM_ADJ2_LAG 2
+#endif
+constexpr int ADJ2_LAG = LBM_ADJ2_LAG;
+static_assert(ADJ2_LAG == 1 || ADJ2_LAG == 2, "step B lags step A by one or two planes");
 __host__ __device__ constexpr bool adj2_in_regs(int i) { return i == 0 || i == 5 || i == 6; }
 __host__ __device__ constexpr int adj2_depth(int i)
 {
-    return adj2_in_regs(i) ? 0 : (ez_of(i) == 1 ? 2 : (ez_of(i) == 0 ? 3 : 4));
+    return adj2_in_regs(i) ? 0 : (ez_of(i) == 1 ? 1 + ADJ2_LAG : (ez_of(i) == 0 ? 2 + ADJ2_LAG : 3 + ADJ2_LAG));
 }
 // first plane slot of each population; used through a constexpr local, so
 // that every index is an immediate (a call at run time would recurse)
@@ -490,12 +499,12 @@ __host__ __device__ constexpr Adj2Layout adj2_layout()
     return l;
 }
 constexpr int ADJ2_SLOTS = adj2_layout().base[Q];
-constexpr size_t ADJ2_SMEM = (size_t)ADJ2_SLOTS * ADJ2_EX * ADJ2_EY * sizeof(float);
+// plane slots, then (lag 2) the mbarrier
 template <bool MACRO> __host__ __device__ constexpr size_t adj2_smem_bytes()
 {
-    return (size_t)ADJ2_SLOTS * ADJ2_EX * adj2_ey<MACRO>() * sizeof(float);
+    return (size_t)ADJ2_SLOTS * ADJ2_EX * adj2_ey<MACRO>() * sizeof(float) + (ADJ2_LAG == 2 ? 16 : 0);
 }
-static_assert(ADJ2_SLOTS == 48, "plane slots of the two-step adjoint");
+static_assert(ADJ2_SLOTS == 32 + 16 * ADJ2_LAG, "plane slots of the two-step adjoint");
 // the largest dim whose 19 dim^3 element offsets fit 32 bits
 constexpr int ADJ2_MAX_DIM = 609;
 
@@ -516,16 +525,17 @@ struct Adj2Args {
     // (reverse streaming), i n - e_i (forward pull), i n (own slot); kernel
     // parameters, so the unrolled loops take them as constant operands
     unsigned off_up[Q], off_down[Q], off_own[Q];
+    int *status;         // bit 1: a bounded wait expired (the launch's results are invalid)
 };
 
 #ifndef LBM_ADJ2_MINB
 #define LBM_ADJ2_MINB 3
 #endif
-// resident blocks per SM of the MACRO variant (no pulled populations in
-// registers: 64 registers without spills; four blocks measured 2% faster
-// than three at 256^3 FP16)
+// resident blocks per SM of the MACRO variant: with lag 1 (48 KB of slots)
+// four (64 registers, no spills; 2% faster than three at 256^3 FP16); with
+// lag 2 (64 KB) three fit
 #ifndef LBM_ADJ2M_MINB
-#define LBM_ADJ2M_MINB (32 / LBM_ADJ2M_EY)
+#define LBM_ADJ2M_MINB (ADJ2_LAG == 2 ? 24 / LBM_ADJ2M_EY : 32 / LBM_ADJ2M_EY)
 #endif
 
 // a_k(s) of one site of step A or B: b = the reverse-streamed adjoint, v =
@@ -554,14 +564,27 @@ __device__ __forceinline__ void adjoint_pull(const S *__restrict__ fwd, const un
 
 // MACRO = true: fwd_a / fwd_b hold the three MODE_STEP_ADJ planes (float) of
 // Q_k / Q_{k-1} instead of the states, and no tau term is formed.
+//
+// Iteration p: step A at plane p (p <= zi1), then step B at plane
+// q = p - ADJ2_LAG (q in [zi0, zi1)).  Step B at plane q reads population i
+// of a_k at plane q + ez_i.  Lag 1: a block barrier between them.  Lag 2:
+// every thread arrives on the mbarrier after step A(p) and waits for the
+// phase after step B(p - 2), whose planes p-1 .. p-3 were complete at the
+// previous wait; a warp can then run at most one plane ahead of the slowest
+// (step A(p+1) while another is in step B(p-2)), which the plane slots'
+// depths 3 / 4 / 5 allow for.
 template <class S, bool MACRO>
 __global__ void __launch_bounds__(ADJ2_EX * adj2_ey<MACRO>(), MACRO ? LBM_ADJ2M_MINB : LBM_ADJ2_MINB)
     adjoint2_kernel(Adj2Args a)
 {
-    extern __shared__ float adj2_smem[];  // [ADJ2_SLOTS][EY][ADJ2_EX]
+    extern __shared__ float adj2_smem[];  // [ADJ2_SLOTS][EY][ADJ2_EX], then the mbarrier
     constexpr int EY = adj2_ey<MACRO>(), TY = EY - 2;
     constexpr int PL = ADJ2_EX * EY;
+    constexpr int LAG = ADJ2_LAG;
     constexpr Adj2Layout LAY = adj2_layout();
+    // slot depth of a population with ez = +1, 0, -1
+    constexpr int DP = 1 + LAG, D0 = 2 + LAG, DM = 3 + LAG;
+    uint64_t *bar = reinterpret_cast<uint64_t *>(adj2_smem + ADJ2_SLOTS * PL);
     const int dim = a.dim;
     const unsigned plane = (unsigned)dim * (unsigned)dim;
     const int lx = (int)threadIdx.x % ADJ2_EX, ly = (int)threadIdx.x / ADJ2_EX;
@@ -585,14 +608,31 @@ __global__ void __launch_bounds__(ADJ2_EX * adj2_ey<MACRO>(), MACRO ? LBM_ADJ2M_
     const float omega = a.omega;
     float dw = 0.f, dl = 0.f;
     const unsigned col = (unsigned)y * (unsigned)dim + (unsigned)x;
-    // register-held populations of a_k: pop 0 of plane p-1, pop 5 of planes
-    // p-1 and p-2 (as of step B of plane p-1)
-    float r0_prev = 0.f, r5_prev1 = 0.f, r5_prev2 = 0.f;
+    // register-held populations of a_k by plane (index k: plane p - k as of
+    // step A of plane p): 6 (ez = +1) back to p - LAG + 1, 0 back to p - LAG,
+    // 5 (ez = -1) back to p - LAG - 1
+    float h6[LAG], h0[LAG + 1], h5[LAG + 2];
+#pragma unroll
+    for (int k = 0; k < LAG; ++k) h6[k] = 0.f;
+#pragma unroll
+    for (int k = 0; k <= LAG; ++k) h0[k] = 0.f;
+#pragma unroll
+    for (int k = 0; k <= LAG + 1; ++k) h5[k] = 0.f;
+    if constexpr (LAG == 2) {
+        if (threadIdx.x == 0) mbar_init(bar, blockDim.x);
+        __syncthreads();
+    }
+    uint32_t phase = 0;
 
-    for (int p = zi0 - 1; p <= zi1; ++p) {
-        float r0, r5, r6;
+    for (int p = zi0 - 1; p <= zi1 - 1 + LAG; ++p) {
+#pragma unroll
+        for (int k = LAG - 1; k > 0; --k) h6[k] = h6[k - 1];
+#pragma unroll
+        for (int k = LAG; k > 0; --k) h0[k] = h0[k - 1];
+#pragma unroll
+        for (int k = LAG + 1; k > 0; --k) h5[k] = h5[k - 1];
         // ---- step A: a_k at (x, y, p) of the ext tile
-        {
+        if (p <= zi1) {
             float b[Q];
             const unsigned site = (unsigned)p * plane + col;
             uint8_t b8 = M_WALL;
@@ -619,22 +659,22 @@ __global__ void __launch_bounds__(ADJ2_EX * adj2_ey<MACRO>(), MACRO ? LBM_ADJ2M_
                     dl += l;
                 }
             }
-            const int m2 = p & 1, m3 = p % 3, m4 = p & 3;
+            const int mp = p % DP, m0 = p % D0, mm = p % DM;
 #pragma unroll
             for (int i = 0; i < Q; ++i) {
                 if (adj2_in_regs(i)) continue;
-                const int slot = LAY.base[i] + (adj2_depth(i) == 2 ? m2 : (adj2_depth(i) == 3 ? m3 : m4));
+                const int slot = LAY.base[i] + (ez_of(i) == 1 ? mp : (ez_of(i) == 0 ? m0 : mm));
                 adj2_smem[slot * PL + threadIdx.x] = b[i];
             }
-            r0 = b[0];
-            r5 = b[5];
-            r6 = b[6];
+            h0[0] = b[0];
+            h5[0] = b[5];
+            h6[0] = b[6];
         }
-        // ---- step B: a_{k-1} at (x, y, p - 1) of the owned tile.  Its
-        // forward values do not depend on step A: loaded before the barrier,
+        // ---- step B: a_{k-1} at (x, y, q) of the owned tile.  Its forward
+        // values do not depend on step A: loaded before the barrier (lag 1),
         // they arrive while the block waits there.
-        const int q = p - 1;
-        const bool do_b = owned && q >= zi0;
+        const int q = p - LAG;
+        const bool do_b = owned && q >= zi0 && q < zi1;
         const unsigned site_b = (unsigned)q * plane + col;
         float mb[3];
         S vb[MACRO ? 1 : Q];
@@ -650,22 +690,23 @@ __global__ void __launch_bounds__(ADJ2_EX * adj2_ey<MACRO>(), MACRO ? LBM_ADJ2M_
                 adjoint_pull<S>(fwd_b, a.off_down, site_b, vb);
             }
         }
-        __syncthreads();
+        if constexpr (LAG == 1) __syncthreads();
+        else mbar_arrive(bar);
         if (do_b) {
             const unsigned site = site_b;
             const uint8_t b8 = b8b;
-            // plane q + ez_i of population i: p (ez = +1), p - 1 (0), p - 2 (-1)
-            const int m2 = p & 1, m3 = (p + 2) % 3, m4 = (p + 2) & 3;
+            // plane q + ez_i of population i
+            const int mp = (q + 1) % DP, m0 = q % D0, mm = (q + DM - 1) % DM;
             float b[Q];
 #pragma unroll
             for (int i = 0; i < Q; ++i) {
                 if (adj2_in_regs(i)) continue;
-                const int slot = LAY.base[i] + (adj2_depth(i) == 2 ? m2 : (adj2_depth(i) == 3 ? m3 : m4));
+                const int slot = LAY.base[i] + (ez_of(i) == 1 ? mp : (ez_of(i) == 0 ? m0 : mm));
                 b[i] = adj2_smem[slot * PL + (ly + ey_of(i)) * ADJ2_EX + (lx + ex_of(i))];
             }
-            b[0] = r0_prev;
-            b[5] = r5_prev2;
-            b[6] = r6;
+            b[0] = h0[LAG];
+            b[5] = h5[LAG + 1];
+            b[6] = h6[LAG - 1];
             float d = 0.f, l = 0.f;
             const float lidv = (b8 & M_FRONT) ? lid[col] : 0.f;
             if constexpr (MACRO) adjoint_site_macro<float>(b, b8, mb[0], mb[1], mb[2], lidv, omega, l);
@@ -675,9 +716,16 @@ __global__ void __launch_bounds__(ADJ2_EX * adj2_ey<MACRO>(), MACRO ? LBM_ADJ2M_
 #pragma unroll
             for (int i = 0; i < Q; ++i) a.aout[site + a.off_own[i]] = b[i];
         }
-        r0_prev = r0;
-        r5_prev2 = r5_prev1;
-        r5_prev1 = r5;
+        if constexpr (LAG == 2) {
+            // bounded: on expiry flag the launch and leave the loop (every
+            // thread then expires at this or the next phase and reaches the
+            // block reduction below)
+            if (!mbar_wait_bounded(bar, phase & 1u, kWaitLimit)) {
+                atomicOr(a.status, 2);
+                break;
+            }
+            ++phase;
+        }
     }
     // one MOVING site per column, in one chunk: a single writer per column
     if (owned && zi0 <= dim - 2 && dim - 2 < zi1) a.grad_lid[col] += (double)dl;

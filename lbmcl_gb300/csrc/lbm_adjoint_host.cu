@@ -199,6 +199,7 @@ cudaError_t adjoint_two_steps(const lbm_t *h, const void *fwd_a, const void *fwd
         a.off_own[i] = (unsigned)base;
     }
     a.omega = (float)h->inv_tau;
+    a.status = h->status;
     const unsigned grid = adj2_grid(h, a.ntx, a.nty, macro);
     switch (h->prec) {
     case LBM_FP32: return macro ? run_adjoint2<float, true>(a, grid, h->stream) : run_adjoint2<float, false>(a, grid, h->stream);
@@ -774,6 +775,11 @@ int lbm_adjoint_backward(lbm_t *h, double dloss, double *grad_tau, double *grad_
     }
     ADJ_CUDA(cudaEventRecord(h->ev_last, st));
     ADJ_CUDA(cudaStreamSynchronize(st));
+    int status = 0;
+    ADJ_CUDA(cudaMemcpy(&status, h->status, sizeof(int), cudaMemcpyDeviceToHost));
+    if (status & 2)
+        return fail(LBM_ETIMEOUT, "lbm_adjoint_backward: a bounded wait of the two-step adjoint expired; "
+                                  "the gradients are not valid");
     double dw = 0.0;
     for (double v : tau) dw += v;
     // omega = 1 / tau

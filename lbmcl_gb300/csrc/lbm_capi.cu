@@ -607,6 +607,7 @@ int lbm_sync(lbm_t *h)
     int st = 0;
     LBM_CUDA(cudaMemcpy(&st, h->status, sizeof(int), cudaMemcpyDeviceToHost));
     if (st & 1) return fail(LBM_EDIVERGED, "lbm_sync: a density <= 0 or NaN was seen (simulation diverged)");
+    if (st & 2) return fail(LBM_ETIMEOUT, "lbm_sync: a kernel's bounded wait expired; its results are not valid");
     return LBM_OK;
 }
 

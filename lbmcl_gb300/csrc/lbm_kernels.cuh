@@ -918,6 +918,12 @@ __device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, uint32
                  "l"(src), "r"(bytes), "r"(smem_addr(bar))
                  : "memory");
 }
+// one arrival (release semantics at CTA scope: this thread's earlier shared
+// memory accesses are visible to the threads that wait for the phase)
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
 __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
 {
     uint32_t ok;
