@@ -476,9 +476,13 @@ template <bool MACRO> __host__ __device__ constexpr int adj2_ey() { return MACRO
 // them; 2 = an mbarrier whose arrival (after step A of plane p) and wait
 // (after step B of plane p - 2) enclose step B's work, so a block's warps
 // drift by up to one plane instead of meeting at every barrier; each
-// population then needs one more plane slot.
+// population then needs one more plane slot.  Lag 2 measured slower at
+// 256^3 FP16 (stored points 0.647 against 0.622 ms per backward iteration,
+// full states 0.907 against 0.715): the barrier stalls go, but three blocks
+// per SM instead of four leave the kernel as bound by load latency as
+// before (ncu: long-scoreboard 5.4 stalls per issue either way).
 #ifndef LBM_ADJ2_LAG
-#define LBM_ADJ2_LAG 2
+#define LBM_ADJ2_LAG 1
 #endif
 constexpr int ADJ2_LAG = LBM_ADJ2_LAG;
 static_assert(ADJ2_LAG == 1 || ADJ2_LAG == 2, "step B lags step A by one or two planes");

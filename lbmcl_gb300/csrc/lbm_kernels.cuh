@@ -1202,7 +1202,7 @@ __global__ void init_kernel(InitArgs a)
 
 // Seeded N(0, sigma^2) noise on the initial populations of the FLUID sites
 // (x, y, z in [2, dim-3]), run after init_kernel: the thread of FLUID site t
-// draws its ten sample pairs (populations 2m, 2m+1 <- pair m) and writes the
+// draws its five sample blocks (populations 4g .. 4g+3 <- block g) and writes the
 // 19 slots (t - e_q, q) of P_{-1} that stream into t (in place: t's own
 // slots (t, q)), each slot having this one writer: the equilibrium at rest
 // (w_q; deviation 0) plus sigma z.  sigma z is one single-precision product
@@ -1221,14 +1221,14 @@ __global__ void noise_kernel(InitArgs a)
     S *f = static_cast<S *>(a.f);
     const Weights<C> W = make_weights<C>();
 #pragma unroll
-    for (int p = 0; p < (Q + 1) / 2; ++p) {
-        float z0, z1;
-        gauss_pair(a.seed, t, (uint32_t)p, z0, z1);
+    for (int g = 0; g < (Q + 3) / 4; ++g) {
+        float zb[4];
+        gauss_block(a.seed, t, (uint32_t)g, zb);
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int q = 2 * p + h;
+        for (int h = 0; h < 4; ++h) {
+            const int q = 4 * g + h;
             if (q >= Q) break;
-            const float zq = h ? z1 : z0;
+            const float zq = zb[h];
             const ptrdiff_t sh = a.in_place ? 0
                                : (ptrdiff_t)ex_of(q) + (ptrdiff_t)ey_of(q) * dim + (ptrdiff_t)ez_of(q) * dim * dim;
             S *dst = f + (size_t)q * a.n + (size_t)((ptrdiff_t)t - sh);

@@ -1,17 +1,17 @@
 // lbm_noise.cuh -- seeded Gaussian perturbation of the initial populations.
 //
-// Two N(0,1) samples per (seed, site, pair): Philox4x32-10 (Salmon, Moraes,
-// Dror, Shaw, SC'11) on the counter (site_lo, site_hi, pair, block); each
-// 32-bit output word is one attempt of Marsaglia's polar method (its low and
-// high 16 bits give the uniform pair), so one block offers four attempts and
-// a warp rarely needs a second block; an accepted attempt gives both
-// normals.  Populations 2m and 2m+1 of a site take the two samples of pair m.
-// The natural logarithm is summed from the atanh series.  Every
-// floating-point step is an explicit IEEE single-precision operation (no
-// contraction, no library transcendental), so a CPU implementation of the
-// same recipe gets the same bits.  Single precision because FP64 runs at a
-// small fraction of the FP32 rate on GB300 and the samples only perturb the
-// initial state.
+// N(0,1) samples per (seed, site): Philox4x32-10 (Salmon, Moraes, Dror,
+// Shaw, SC'11) on the counter (site_lo, site_hi, block, 0) gives four 32-bit
+// words; each pair of words is one Box-Muller draw (Box and Muller, 1958):
+// a radius sqrt(-2 ln u1) from 23 bits of the first word, an angle from 24
+// bits of the second, and the pair (r cos theta, r sin theta).  Block g
+// feeds sample pairs 2g and 2g+1; populations 2m and 2m+1 of a site take
+// pair m.  The logarithm is summed from the atanh series, sine and cosine
+// from their Taylor series on a quarter turn.  Every floating-point step is
+// an explicit IEEE single-precision operation (no contraction, no library
+// transcendental), so a CPU implementation of the same recipe gets the same
+// bits.  Single precision because FP64 runs at a small fraction of the FP32
+// rate on GB300 and the samples only perturb the initial state.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -68,52 +68,52 @@ __device__ __forceinline__ float series_logf(float x)
     return __fadd_rn(__fmul_rn((float)e, ln2), __fmul_rn(__fmul_rn(2.0f, s), acc));
 }
 
-// uniform in (-1, 1) from 16 random bits: (a + 1/2) / 2^15 - 1, exact
-__device__ __forceinline__ float sym_uniform16(uint32_t a)
+// cos and sin of the angle 2 pi (k / 4 + 1 / 8 + x / (2 pi)), x in
+// (-pi/4, pi/4), k in 0..3: the quarter turn k, then pi/4 + x from the Taylor
+// series of cos x (to x^10) and sin x (to x^9) and the rotation by pi/4.
+__device__ __forceinline__ void quarter_turn_cs(uint32_t k, float x, float &c, float &s)
 {
-    return __fsub_rn(__fmul_rn(__fadd_rn((float)a, 0.5f), 1.0f / 32768.0f), 1.0f);
+    const float x2 = __fmul_rn(x, x);
+    float sp = 1.0f / 362880.0f;
+    sp = __fadd_rn(-1.0f / 5040.0f, __fmul_rn(x2, sp));
+    sp = __fadd_rn(1.0f / 120.0f, __fmul_rn(x2, sp));
+    sp = __fadd_rn(-1.0f / 6.0f, __fmul_rn(x2, sp));
+    const float sn = __fadd_rn(x, __fmul_rn(__fmul_rn(x, x2), sp));
+    float cp = -1.0f / 3628800.0f;
+    cp = __fadd_rn(1.0f / 40320.0f, __fmul_rn(x2, cp));
+    cp = __fadd_rn(-1.0f / 720.0f, __fmul_rn(x2, cp));
+    cp = __fadd_rn(1.0f / 24.0f, __fmul_rn(x2, cp));
+    cp = __fadd_rn(-0.5f, __fmul_rn(x2, cp));
+    const float cs = __fadd_rn(1.0f, __fmul_rn(x2, cp));
+    const float h = 0.707106781f;  // sqrt(1/2)
+    const float c0 = __fmul_rn(h, __fsub_rn(cs, sn)), s0 = __fmul_rn(h, __fadd_rn(cs, sn));
+    c = (k == 0) ? c0 : (k == 1) ? -s0 : (k == 2) ? -c0 : s0;
+    s = (k == 0) ? s0 : (k == 1) ? c0 : (k == 2) ? -s0 : -c0;
 }
 
-// The two samples of pair `pair` of a site (at most 64 attempts).
-__device__ __forceinline__ void gauss_pair(uint64_t seed, uint64_t site, uint32_t pair, float &z0, float &z1)
+// One Box-Muller pair from two 32-bit words: u1 = (w0 >> 9 + 1/2) / 2^23 in
+// (0, 1) (exact), the angle's quarter turn from the top two bits of w1 and
+// its offset in the quarter from the next 22, (f + 1/2) / 2^22 (exact).
+__device__ __forceinline__ void box_muller(uint32_t w0, uint32_t w1, float &z0, float &z1)
 {
-    const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
-    for (uint32_t block = 0; block < 16; ++block) {
-        uint32_t c[4] = {(uint32_t)site, (uint32_t)(site >> 32), pair, block};
-        philox4x32_10(c, k0, k1);
-        // the first accepted attempt of the four, found by selects; the
-        // logarithm, division and square root then run once
-        float v1 = 0.0f, v2 = 0.0f, s = 0.0f;
-        bool found = false;
-#pragma unroll
-        for (int a = 3; a >= 0; --a) {
-            const float w1 = sym_uniform16(c[a] & 0xffffu);
-            const float w2 = sym_uniform16(c[a] >> 16);
-            const float sa = __fadd_rn(__fmul_rn(w1, w1), __fmul_rn(w2, w2));
-            const bool ok = sa < 1.0f && sa != 0.0f;
-            v1 = ok ? w1 : v1;
-            v2 = ok ? w2 : v2;
-            s = ok ? sa : s;
-            found |= ok;
-        }
-        if (found) {
-            const float t = __fdiv_rn(__fmul_rn(-2.0f, series_logf(s)), s);
-            const float r = __fsqrt_rn(t);
-            z0 = __fmul_rn(v1, r);
-            z1 = __fmul_rn(v2, r);
-            return;
-        }
-    }
-    z0 = 0.0f;
-    z1 = 0.0f;
+    const float u1 = __fmul_rn(__fadd_rn((float)(w0 >> 9), 0.5f), 1.0f / 8388608.0f);
+    const float r = __fsqrt_rn(__fmul_rn(-2.0f, series_logf(u1)));
+    const float fq = __fmul_rn(__fadd_rn((float)((w1 >> 8) & 0x3fffffu), 0.5f), 1.0f / 4194304.0f);
+    const float x = __fmul_rn(__fsub_rn(fq, 0.5f), 1.57079637f);  // (fq - 1/2) pi/2
+    float c, s;
+    quarter_turn_cs(w1 >> 30, x, c, s);
+    z0 = __fmul_rn(r, c);
+    z1 = __fmul_rn(r, s);
 }
 
-// The sample of population q of a site.
-__device__ __forceinline__ float gauss(uint64_t seed, uint64_t site, uint32_t q)
+// The four samples of block g of a site: pairs 2g (z[0], z[1]) and 2g + 1
+// (z[2], z[3]).
+__device__ __forceinline__ void gauss_block(uint64_t seed, uint64_t site, uint32_t g, float (&z)[4])
 {
-    float z0, z1;
-    gauss_pair(seed, site, q >> 1, z0, z1);
-    return (q & 1u) ? z1 : z0;
+    uint32_t c[4] = {(uint32_t)site, (uint32_t)(site >> 32), g, 0u};
+    philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+    box_muller(c[0], c[1], z[0], z[1]);
+    box_muller(c[2], c[3], z[2], z[3]);
 }
 
 }  // namespace lbm

@@ -128,39 +128,57 @@ float lbmo_logf(float x)
 
 double lbmo_log(double x) { return (double)lbmo_logf((float)x); }
 
-/* Uniform in (-1, 1) from 16 random bits: (a + 1/2) / 2^15 - 1, exact in float. */
-static inline float lbmo_sym_uniform16(uint32_t a)
+/* cos and sin of 2 pi (k/4 + 1/8) + x, x in (-pi/4, pi/4), k in 0..3:
+ * Taylor series of cos x (to x^10) and sin x (to x^9), the rotation by pi/4
+ * to pi/4 + x, then the quarter turn k.  IEEE float + - * only. */
+static void lbmo_quarter_turn_cs(uint32_t k, float x, float *c, float *s)
 {
-    return (((float)a + 0.5f) * (1.0f / 32768.0f)) - 1.0f;
+    const float x2 = x * x;
+    float sp = 1.0f / 362880.0f;
+    sp = (-1.0f / 5040.0f) + x2 * sp;
+    sp = (1.0f / 120.0f) + x2 * sp;
+    sp = (-1.0f / 6.0f) + x2 * sp;
+    const float sn = x + (x * x2) * sp;
+    float cp = -1.0f / 3628800.0f;
+    cp = (1.0f / 40320.0f) + x2 * cp;
+    cp = (-1.0f / 720.0f) + x2 * cp;
+    cp = (1.0f / 24.0f) + x2 * cp;
+    cp = -0.5f + x2 * cp;
+    const float cs = 1.0f + x2 * cp;
+    const float h = 0.707106781f; /* sqrt(1/2) */
+    const float c0 = h * (cs - sn), s0 = h * (cs + sn);
+    *c = (k == 0) ? c0 : (k == 1) ? -s0 : (k == 2) ? -c0 : s0;
+    *s = (k == 0) ? s0 : (k == 1) ? c0 : (k == 2) ? -s0 : -c0;
 }
 
-/* Two standard normals for (seed, site, pair) by the Marsaglia polar method:
- * Philox4x32-10 on the counter (site_lo, site_hi, pair, block); each 32-bit
- * output word is one attempt (its low and high 16 bits give v1, v2), so a
- * block offers four attempts; the first accepted attempt gives both
- * v1 r and v2 r, r = sqrt(-2 ln s / s).  Single precision, IEEE + - * /
- * sqrt only; at most 64 attempts, so the loop always ends. */
+/* One Box-Muller pair from two 32-bit words: u1 = ((w0 >> 9) + 1/2) / 2^23
+ * in (0, 1), r = sqrt(-2 ln u1); the angle's quarter turn from the top two
+ * bits of w1, its offset x = (fq - 1/2) pi/2 from the next 22 bits,
+ * fq = (f + 1/2) / 2^22 (both uniforms exact in float). */
+static void lbmo_box_muller(uint32_t w0, uint32_t w1, float z[2])
+{
+    const float u1 = ((float)(w0 >> 9) + 0.5f) * (1.0f / 8388608.0f);
+    const float r = sqrtf(-2.0f * lbmo_logf(u1));
+    const float fq = ((float)((w1 >> 8) & 0x3fffffu) + 0.5f) * (1.0f / 4194304.0f);
+    const float x = (fq - 0.5f) * 1.57079637f;
+    float c, s;
+    lbmo_quarter_turn_cs(w1 >> 30, x, &c, &s);
+    z[0] = r * c;
+    z[1] = r * s;
+}
+
+/* Two standard normals for (seed, site, pair) by the Box-Muller transform:
+ * Philox4x32-10 on the counter (site_lo, site_hi, pair >> 1, 0); words 0, 1
+ * give pair 2g, words 2, 3 pair 2g + 1 of block g.  Single precision, IEEE
+ * + - * / sqrt only. */
 void lbmo_gauss_pairf(uint64_t seed, uint64_t site, uint32_t pair, float z[2])
 {
     const uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
-    for (uint32_t block = 0; block < 16; ++block) {
-        const uint32_t ctr[4] = {(uint32_t)site, (uint32_t)(site >> 32), pair, block};
-        uint32_t r[4];
-        lbmo_philox4x32_10(ctr, key, r);
-        for (int a = 0; a < 4; ++a) {
-            const float v1 = lbmo_sym_uniform16(r[a] & 0xffffu);
-            const float v2 = lbmo_sym_uniform16(r[a] >> 16);
-            const float s = (v1 * v1) + (v2 * v2);
-            if (s >= 1.0f || s == 0.0f) continue;
-            const float t = (-2.0f * lbmo_logf(s)) / s;
-            const float rt = sqrtf(t);
-            z[0] = v1 * rt;
-            z[1] = v2 * rt;
-            return;
-        }
-    }
-    z[0] = 0.0f;
-    z[1] = 0.0f;
+    const uint32_t ctr[4] = {(uint32_t)site, (uint32_t)(site >> 32), pair >> 1, 0u};
+    uint32_t r[4];
+    lbmo_philox4x32_10(ctr, key, r);
+    const int w = 2 * (int)(pair & 1u);
+    lbmo_box_muller(r[w], r[w + 1], z);
 }
 
 /* The sample of population q of a site: element q & 1 of pair q >> 1. */

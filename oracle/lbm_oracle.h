@@ -62,11 +62,11 @@ typedef struct lbmo_params {
 int lbmo_cell_type(int dim, int x, int y, int z);
 
 /* Standard normal sample for (seed, site, q): Philox4x32-10 counter stream,
- * Marsaglia polar method (both normals of an accepted attempt: populations
- * 2m and 2m+1 share pair m), a self-contained natural logarithm.  Computed
- * with IEEE single-precision + - * / sqrt only, so the GPU library
- * reproduces it bit for bit.  lbmo_gauss returns the same value widened to
- * double; lbmo_gauss_pairf gives both samples of one pair. */
+ * Box-Muller transform (block g of a site gives pairs 2g and 2g+1:
+ * populations 4g .. 4g+3), a self-contained natural logarithm, sine and
+ * cosine.  Computed with IEEE single-precision + - * / sqrt only, so the GPU
+ * library reproduces it bit for bit.  lbmo_gauss returns the same value
+ * widened to double; lbmo_gauss_pairf gives both samples of one pair. */
 void lbmo_gauss_pairf(uint64_t seed, uint64_t site, uint32_t pair, float z[2]);
 float lbmo_gaussf(uint64_t seed, uint64_t site, uint32_t q);
 double lbmo_gauss(uint64_t seed, uint64_t site, uint32_t q);

@@ -145,6 +145,8 @@ def test_gauss_moments(oracle):
     assert abs(z.mean()) < 0.03
     assert abs(z.var() - 1.0) < 0.04
     assert abs((z ** 4).mean() - 3.0) < 0.25
+    stats = pytest.importorskip("scipy.stats")
+    assert stats.kstest(z, "norm").pvalue > 1e-3
     # deterministic and keyed by all of (seed, site, q)
     assert oracle.gauss(1, 2, 3) == oracle.gauss(1, 2, 3)
     assert len({oracle.gauss(1, 2, 3), oracle.gauss(2, 2, 3), oracle.gauss(1, 3, 3), oracle.gauss(1, 2, 4)}) == 4
