@@ -120,6 +120,11 @@ typedef struct lbm_config {
                                   storage too (one step per launch), e.g. to measure the
                                   FP32 adjoint's rounding on the same trajectory; 0: FP64
                                   only for FP64 storage                                     */
+    int order;                 /* summation order of rho and u (FP32 / FP64 storage):
+                                  LBM_ORDER_REFERENCE (the reference's active order,
+                                  kernels.cl:355, 376-378) or LBM_ORDER_SAILFISH (its
+                                  compiled-out Sailfish order, kernels.cl:352-354,
+                                  368-375); the gradient calls need the reference order   */
 } lbm_config;
 
 /* Iteration kernel variants (same results, different data movement). */
@@ -134,6 +139,12 @@ typedef enum lbm_kernel {
                                 LBM_DUMP_F_RAW then holds the current step's layout, and
                                 the lbm_adjoint_* calls are not available                 */
 } lbm_kernel;
+
+/* Summation orders of rho and u (lbm_config.order). */
+typedef enum lbm_order {
+    LBM_ORDER_REFERENCE = 0, /* kernels.cl:355, 376-378 (the reference's active path)   */
+    LBM_ORDER_SAILFISH = 1   /* kernels.cl:352-354, 368-375 (CALCULATION_ORDER_SAILFISH) */
+} lbm_order;
 
 /* Fill *c with the reference CLI defaults (lbm_options.hpp:83-101):
  * dim 8, nu 0.0089, u 0.05, FP32, stride 32. */

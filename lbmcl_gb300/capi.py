@@ -19,6 +19,7 @@ HEADER = os.path.join(os.path.dirname(PKG), "include", "lbm.h")
 FP32, FP64, FP16, BF16 = 0, 1, 2, 3
 PRECISIONS = {"fp32": FP32, "fp64": FP64, "fp16": FP16, "bf16": BF16}
 KERNELS = {"auto": 0, "direct": 1, "staged": 2, "narrow": 3, "aa": 4}
+ORDERS = {"reference": 0, "sailfish": 1}
 DUMP_F, DUMP_RHO, DUMP_U, DUMP_MAP, DUMP_MAP_U8, DUMP_F_RAW = 0, 1, 2, 3, 4, 5
 OK, EINVAL, ENOMEM, ECUDA, ESTATE, EDIVERGED, ETIMEOUT = 0, 1, 2, 3, 4, 5, 6
 Q = 19
@@ -52,6 +53,7 @@ class Config(C.Structure):
         ("graph_iterations", C.c_int),
         ("adjoint_full_states", C.c_int),
         ("adjoint_fp64", C.c_int),
+        ("order", C.c_int),
     ]
 
 
@@ -127,13 +129,14 @@ class Lattice:
     1 = no graphs).  adjoint_full_states: recompute full states in a backward
     sweep without a tau gradient too (default: only the velocity / density
     the adjoint needs).  adjoint_fp64: FP64 adjoint arithmetic over FP32 /
-    16-bit storage.
+    16-bit storage.  order: "reference" | "sailfish" summation order of rho
+    and u (FP32 / FP64).
     """
 
     def __init__(self, dim, viscosity=0.0089, velocity=0.05, precision="fp32", stride=None, lid=None,
                  seed=0, noise_sigma=0.0, tau=0.0, block_threads=0, max_device_bytes=0, device=0,
                  profile_steps=False, kernel=0, stages=0, adjoint_steps=0, adjoint_max_states=0,
-                 graph_iterations=0, adjoint_full_states=False, adjoint_fp64=False):
+                 graph_iterations=0, adjoint_full_states=False, adjoint_fp64=False, order="reference"):
         L = lib()
         c = default_config()
         c.dim = int(dim)
@@ -159,6 +162,7 @@ class Lattice:
         c.graph_iterations = int(graph_iterations)
         c.adjoint_full_states = 1 if adjoint_full_states else 0
         c.adjoint_fp64 = 1 if adjoint_fp64 else 0
+        c.order = ORDERS[order] if isinstance(order, str) else int(order)
         self.cfg = c
         self.dim = int(dim)
         self.n = self.dim ** 3

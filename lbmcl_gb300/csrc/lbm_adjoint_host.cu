@@ -519,6 +519,9 @@ int lbm_adjoint_forward(lbm_t *h, int iterations, int checkpoint_every, double *
     if (h->kernel == LBM_KERNEL_AA)
         return fail(LBM_ESTATE, "lbm_adjoint_forward: the adjoint needs the two-lattice kernels "
                                 "(LBM_KERNEL_AA keeps one lattice in place)");
+    if (h->cfg.order != LBM_ORDER_REFERENCE)
+        return fail(LBM_ESTATE, "lbm_adjoint_forward: the adjoint is linearised in the reference summation "
+                                "order (lbm_config.order = LBM_ORDER_REFERENCE)");
     lbm_adjoint_state &s = h->adj;
     const size_t fbytes = (size_t)lbm::Q * h->n * lbm::storage_bytes(h->prec);
     // drop the previous run's state buffers (the target and work buffers

@@ -174,6 +174,7 @@ lbm::StepArgs step_args(const lbm_t *h, int from, int phase)
     a.gpp = h->gpp;
     a.ngroups = h->ngroups;
     a.stages = h->stages;
+    a.sailfish = h->cfg.order == LBM_ORDER_SAILFISH ? 1 : 0;
     return a;
 }
 lbm::StepArgs step_args(const lbm_t *h, int from) { return step_args(h, from, h->aa_phase); }
@@ -406,6 +407,10 @@ int lbm_init(lbm_t **out, const lbm_config *c)
         return fail(LBM_EINVAL, "lbm_init: adjoint_fp64 %d must be 0 or 1", c->adjoint_fp64);
     if (c->adjoint_full_states < 0 || c->adjoint_full_states > 1)
         return fail(LBM_EINVAL, "lbm_init: adjoint_full_states %d must be 0 or 1", c->adjoint_full_states);
+    if (c->order < LBM_ORDER_REFERENCE || c->order > LBM_ORDER_SAILFISH)
+        return fail(LBM_EINVAL, "lbm_init: unknown summation order %d", c->order);
+    if (c->order == LBM_ORDER_SAILFISH && c->precision != LBM_FP32 && c->precision != LBM_FP64)
+        return fail(LBM_EINVAL, "lbm_init: the Sailfish summation order needs FP32 or FP64 storage");
     if (c->graph_iterations < 0 || c->graph_iterations > 256 || (c->graph_iterations > 1 && c->graph_iterations % 2))
         return fail(LBM_EINVAL, "lbm_init: graph_iterations %d must be 0, 1 or an even number <= 256",
                     c->graph_iterations);

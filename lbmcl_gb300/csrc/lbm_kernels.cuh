@@ -148,16 +148,18 @@ struct SiteOut {
 };
 
 // Exact-order FP32 / FP64 site update.  COLLIDE = false only forms moments.
+// sf: rho and u in the Sailfish summation order (block-uniform).
 template <class T, bool COLLIDE>
 __device__ __forceinline__ void site_exact(T (&f)[Q], uint8_t b, T lidv, T inv_tau, const Weights<T> &W,
-                                           SiteOut &o)
+                                           SiteOut &o, bool sf)
 {
     using O = X<T>;
     o.macro = false;
     o.bad = false;
     if (b == 0) {  // FLUID
         T r, ux, uy, uz;
-        moments_exact(f, r, ux, uy, uz);
+        if (sf) moments_sailfish(f, r, ux, uy, uz);
+        else moments_exact(f, r, ux, uy, uz);
         o.macro = true;
         o.bad = !(r > (T)0);
         o.r = r; o.ux = ux; o.uy = uy; o.uz = uz;
@@ -172,9 +174,14 @@ __device__ __forceinline__ void site_exact(T (&f)[Q], uint8_t b, T lidv, T inv_t
     if (b == M_FRONT) {
         // moving lid (kernels.cl:343-349, 355, 362-367, 393-398)
         f[5] = f[6]; f[11] = f[17]; f[12] = f[18]; f[13] = f[15]; f[14] = f[16];
-        T r = f[0];
+        T r;
+        if (sf) {
+            r = rho_sailfish(f);
+        } else {
+            r = f[0];
 #pragma unroll
-        for (int i = 1; i < Q; ++i) r = O::add(r, f[i]);
+            for (int i = 1; i < Q; ++i) r = O::add(r, f[i]);
+        }
         o.macro = true;
         o.bad = !(r > (T)0);
         o.r = r; o.ux = lidv; o.uy = 0; o.uz = 0;
@@ -484,7 +491,7 @@ __device__ __forceinline__ void update_general(S (&fs)[Q][V], typename MapWord<V
             C f[Q];
 #pragma unroll
             for (int i = 0; i < Q; ++i) f[i] = fs[i][k];
-            site_exact<C, MODE != MODE_REDUCE>(f, b, lidv, inv_tau, W, o);
+            site_exact<C, MODE != MODE_REDUCE>(f, b, lidv, inv_tau, W, o, a.sailfish != 0);
 #pragma unroll
             for (int i = 0; i < Q; ++i) fs[i][k] = f[i];
         }
@@ -521,7 +528,7 @@ __device__ __forceinline__ void update_vector(S (&fs)[Q][V], typename MapWord<V>
                     C f[Q];
 #pragma unroll
                     for (int i = 0; i < Q; ++i) f[i] = fs[i][k + h];
-                    site_exact<C, MODE != MODE_REDUCE>(f, 0, (C)0, inv_tau, W, o[h]);
+                    site_exact<C, MODE != MODE_REDUCE>(f, 0, (C)0, inv_tau, W, o[h], a.sailfish != 0);
 #pragma unroll
                     for (int i = 0; i < Q; ++i) fs[i][k + h] = f[i];
                 }

@@ -56,6 +56,9 @@ typedef struct lbmo_params {
     double noise_sigma;      /* 0: no noise; FP32 adds (float)sigma * z in float,
                               * FP64 adds sigma * z in double                    */
     int threads;             /* OpenMP threads, 0: runtime default                */
+    int order;               /* 0: the reference's summation order of rho and u
+                              * (kernels.cl:355, 376-378); 1: its compiled-out
+                              * Sailfish order (kernels.cl:352-354, 368-375)    */
 } lbmo_params;
 
 /* Reference cell type of site (x,y,z) (kernels.cl:236-266). */

@@ -132,15 +132,27 @@ void SFX(lbmo_compute)(const lbmo_params *p, REAL *f_stream, const REAL *f_colli
                     f[14] = f[16];
                 }
 
-                /* density, index order (kernels.cl:355) */
-                REAL r = f[0];
-                for (int i = 1; i < LBMO_Q; ++i) r = r + f[i];
+                /* density, index order (kernels.cl:355), or the Sailfish
+                 * order (kernels.cl:352-354) */
+                REAL r;
+                if (p->order == 1) {
+                    r = f[5] + f[11] + f[12] + f[14] + f[13] + f[0] + f[1] + f[2] + f[7] + f[8] + f[4] +
+                        f[10] + f[9] + f[6] + f[15] + f[16] + f[18] + f[17] + f[3];
+                } else {
+                    r = f[0];
+                    for (int i = 1; i < LBMO_Q; ++i) r = r + f[i];
+                }
 
                 REAL ux, uy, uz;
                 if (lbmo_is_moving(ct)) {
                     ux = SFX(lid_at)(p, x, y);
                     uy = (REAL)0.0;
                     uz = (REAL)0.0;
+                } else if (p->order == 1) {
+                    /* kernels.cl:368-375, left to right */
+                    ux = (f[11] - f[13] + f[1] + f[7] - f[8] + f[10] - f[9] + f[15] - f[17] - f[3]) / r;
+                    uy = (f[12] - f[14] + f[2] + f[7] + f[8] - f[4] - f[10] - f[9] + f[16] - f[18]) / r;
+                    uz = (-f[5] - f[11] - f[12] - f[14] - f[13] + f[6] + f[15] + f[16] + f[18] + f[17]) / r;
                 } else {
                     /* kernels.cl:376-378 */
                     ux = ((f[1] + f[7] + f[10] + f[11] + f[15]) - (f[3] + f[8] + f[9] + f[13] + f[17])) / r;

@@ -42,6 +42,7 @@ class _Params(C.Structure):
         ("seed", C.c_uint64),
         ("noise_sigma", C.c_double),
         ("threads", C.c_int),
+        ("order", C.c_int),
     ]
 
 
@@ -102,7 +103,7 @@ class OracleLattice:
     """
 
     def __init__(self, dim, viscosity, velocity, precision="f32", stride=None, lid=None,
-                 seed=0, noise_sigma=0.0, threads=0):
+                 seed=0, noise_sigma=0.0, threads=0, order="reference"):
         self.dim = int(dim)
         self.n = self.dim ** 3
         self.dtype = np.float32 if precision == "f32" else np.float64
@@ -114,7 +115,8 @@ class OracleLattice:
             assert self._lid.size == self.dim * self.dim
         self.p = _Params(self.dim, stride_log2(stride), float(viscosity), float(velocity),
                          self._lid.ctypes.data_as(C.POINTER(C.c_double)) if self._lid is not None else None,
-                         int(seed) & 0xFFFFFFFFFFFFFFFF, float(noise_sigma), int(threads))
+                         int(seed) & 0xFFFFFFFFFFFFFFFF, float(noise_sigma), int(threads),
+                         1 if order == "sailfish" else 0)
         self.fa = np.empty(self.n * Q, self.dtype)
         self.fb = np.empty(self.n * Q, self.dtype)
         self.rho = np.empty(self.n, self.dtype)

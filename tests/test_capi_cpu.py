@@ -54,6 +54,8 @@ def _init(libonly, **kw):
     (dict(adjoint_max_states=-2), "adjoint_max_states"),
     (dict(graph_iterations=3), "graph_iterations"),
     (dict(graph_iterations=512), "graph_iterations"),
+    (dict(order=2), "summation order"),
+    (dict(order=1, precision=3), "Sailfish"),   # FP16 storage: its own deviation sums
 ])
 def test_init_rejects_bad_arguments(libonly, kw, frag):
     rc, msg = _init(libonly, **kw)

@@ -89,6 +89,21 @@ def test_oracle_vs_sailfish_32(oracle):
     assert w["mse_rho"] < 1e-11 and w["mse_v"] < 1e-12, w
 
 
+def test_sailfish_order_is_closer_to_the_sailfish_data(oracle):
+    """The compiled-out Sailfish summation order (kernels.cl:352-354,
+    368-375) against the golden Sailfish runs: closer than the reference's
+    active order at both sizes (not bit-equal: Sailfish's collision is
+    evaluated in its own order too)."""
+    for dim, steps, every, name, lim in [(8, list(range(0, 11)), 1, "sailfish_ldc8.npz", (4e-7, 2e-7)),
+                                         (32, [20, 500], 20, "sailfish_ldc32.npz", (2e-6, 5e-7))]:
+        gold = np.load(os.path.join(GOLD, name))
+        ws = _verify(dim, oracle.OracleLattice(dim, 0.0089, 0.05, "f32", dim, order="sailfish"), gold, steps, every)
+        wr = _verify(dim, oracle.OracleLattice(dim, 0.0089, 0.05, "f32", dim), gold, steps, every)
+        assert ws["mae_rho"] < lim[0] and ws["mae_v"] < lim[1], (dim, ws)
+        assert ws["mae_rho"] <= wr["mae_rho"] and ws["mae_v"] <= wr["mae_v"], (dim, ws, wr)
+        assert ws["mse_rho"] < wr["mse_rho"], (dim, ws, wr)
+
+
 @pytest.mark.parametrize("prec", ["f32", "f64"])
 def test_oracle_vs_ref_live(oracle, prec):
     if not oracle.ref_available(prec):

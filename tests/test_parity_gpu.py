@@ -56,6 +56,44 @@ def test_f_after_each_step(capi, oracle, prec, dim, stride, kernel):
             np.testing.assert_array_equal(bits(L.u()), bits(o.u))
 
 
+@pytest.mark.parametrize("kernel", ["direct", "narrow", "staged", "aa"])
+@pytest.mark.parametrize("prec", ["f32", "f64"])
+def test_sailfish_order(capi, oracle, prec, kernel):
+    """The Sailfish summation order of rho and u (kernels.cl:352-354,
+    368-375; compiled out in the reference) against the oracle's, bit for
+    bit, with a lid profile, noise and macro output; it differs from the
+    reference order's run, and its reductions follow it too."""
+    if prec == "f64" and kernel == "narrow":
+        pytest.skip("no narrow FP64 variant")
+    rng = np.random.default_rng(5)
+    dim = 24
+    lid = 0.05 + 0.01 * rng.standard_normal(dim * dim)
+    kw = dict(lid=lid, seed=99, noise_sigma=1e-4)
+    o = oracle.OracleLattice(dim, 0.01, 0.05, prec, 8, order="sailfish", **kw)
+    r = oracle.OracleLattice(dim, 0.01, 0.05, prec, 8, **kw)
+    with capi.Lattice(dim, 0.01, 0.05, precision=GPU_PREC[prec], stride=8, kernel=kernel, order="sailfish",
+                      **kw) as L:
+        for chunk in (1, 5, 34):
+            o.step(chunk, every=chunk)
+            r.step(chunk, every=chunk)
+            L.step(chunk, every=chunk)
+            g = L.f()
+            assert np.array_equal(bits(g), bits(o.state)), f"after {o.it}: not bit-identical"
+            np.testing.assert_array_equal(bits(L.rho()), bits(o.rho))
+            np.testing.assert_array_equal(bits(L.u()), bits(o.u))
+        assert not np.array_equal(bits(o.state), bits(r.state))
+        m = L.reduce()[0]
+        rho = o.rho[~np.isnan(o.rho)].astype(np.float64)
+        assert abs(m - rho.sum()) <= 1e-9 * rho.sum()
+
+
+def test_sailfish_order_refuses_the_adjoint(capi):
+    with capi.Lattice(16, precision="fp32", order="sailfish") as L:
+        L.adjoint_set_loss(8, np.zeros(16 * 16))
+        with pytest.raises(capi.LbmError, match="summation order"):
+            L.adjoint_forward(4, 2)
+
+
 @pytest.mark.parametrize("kernel", ["direct", "staged", "aa"])
 @pytest.mark.parametrize("prec", ["f32", "f64"])
 def test_lid_profile_noise_and_macro_every(capi, oracle, prec, kernel):
