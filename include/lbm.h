@@ -125,6 +125,12 @@ typedef struct lbm_config {
                                   kernels.cl:355, 376-378) or LBM_ORDER_SAILFISH (its
                                   compiled-out Sailfish order, kernels.cl:352-354,
                                   368-375); the gradient calls need the reference order   */
+    int adjoint_kernel;        /* data movement of the FP32 adjoint's two-step kernel in
+                                  the stored-point sweep: 0 = tuned default (DIRECT),
+                                  LBM_KERNEL_DIRECT = per-thread loads from HBM,
+                                  LBM_KERNEL_STAGED = each plane's inputs staged in shared
+                                  memory by tiled TMA loads (dim % 4 == 0); the same
+                                  per-site arithmetic                                      */
 } lbm_config;
 
 /* Iteration kernel variants (same results, different data movement). */

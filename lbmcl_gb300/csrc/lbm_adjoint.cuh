@@ -27,6 +27,8 @@
 //  bounce-back: a_j = b_opp(j);  CORNER: a_j = b_j;  WALL: a = 0.
 #pragma once
 
+#include <cuda.h>
+
 #include "lbm_kernels.cuh"
 
 namespace lbm {
@@ -734,6 +736,219 @@ __global__ void __launch_bounds__(ADJ2_EX * adj2_ey<MACRO>(), MACRO ? LBM_ADJ2M_
     // one MOVING site per column, in one chunk: a single writer per column
     if (owned && zi0 <= dim - 2 && dim - 2 < zi1) a.grad_lid[col] += (double)dl;
     if constexpr (!MACRO) block_reduce_add((double)dw, a.tau_acc);
+}
+
+// ---------------------------------------------------------------------------
+// The stored-point two-step adjoint with its inputs staged by TMA.
+//
+// Same tiles, z-chunks, plane slots and per-site arithmetic as
+// adjoint2_kernel<S, true>, but no thread loads its inputs from global
+// memory: for every plane p one thread issues 25 tiled TMA loads
+// (cp.async.bulk.tensor) of 40 x 8 floats into one stage of a two-stage
+// shared-memory ring -- the 19 populations of a_{k+1} at (x + e_ix, y + e_iy,
+// p + e_iz), the three point planes of Q_k at plane p (step A) and those of
+// Q_{k-1} at plane p - 1 (step B) -- completing on that stage's mbarrier.
+// The stage of plane p + 2 is issued as soon as every thread has read the
+// stage of plane p (the block barrier between step A and step B), so the
+// loads of the next plane are in flight while the block computes.
+//
+// Boxes start at xs = the ext tile's first x - 1 rounded down to a multiple
+// of 4 (16 bytes: the TMA alignment of the innermost coordinate); 40 columns
+// cover the 34 that the tile reads.  Coordinates outside the lattice (x or y
+// in {-4 .. -1} or >= dim, planes -1 and dim) are filled with zeros by the
+// TMA unit; no site that reads them is a non-wall site.
+//
+// Waits on the stage barriers are bounded.  Every thread folds its wait's
+// outcome into the block barrier (__syncthreads_or), so an expired wait
+// stops the whole block before step B writes anything; it sets bit 1 of the
+// status word, the issuing thread drains the copies still in flight (again
+// bounded) and the block returns.
+// ---------------------------------------------------------------------------
+constexpr int ADJ2T_BW = 40;                         // box columns (floats)
+constexpr int ADJ2T_NB = Q + 6;                      // boxes per stage
+constexpr int ADJ2T_BOX = ADJ2T_BW * ADJ2_EY;        // floats per box
+constexpr int ADJ2T_STAGE = ADJ2T_NB * ADJ2T_BOX;    // floats per stage
+constexpr int ADJ2T_NS = 2;                          // stages
+constexpr size_t adj2t_smem_bytes()
+{
+    return (size_t)ADJ2T_NS * ADJ2T_STAGE * sizeof(float) + (size_t)ADJ2_SLOTS * ADJ2_EX * ADJ2_EY * sizeof(float) +
+           (size_t)ADJ2T_NS * sizeof(uint64_t);
+}
+static_assert((ADJ2T_BOX * sizeof(float)) % 128 == 0, "TMA destinations stay 128-byte aligned");
+
+// One 4-D tiled TMA load (coordinates x, y, z, w; x fastest) into shared
+// memory, completing on bar.  x * 4 bytes must be a multiple of 16.
+__device__ __forceinline__ void tma_load_4d(void *dst, const CUtensorMap *map, int x, int y, int z, int w,
+                                            uint64_t *bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
+        "%5}], [%6];" ::"r"(smem_addr(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(w), "r"(smem_addr(bar))
+        : "memory");
+}
+
+// map_a: a_{k+1} as (dim, dim, dim, 19) floats; map_pa / map_pb: the point
+// planes of Q_k / Q_{k-1} as (dim, dim, dim, 3) floats; all with 40 x 8 x 1
+// x 1 boxes.  (A template so that every translation unit that includes
+// this header can hold it.)
+template <int NS>
+__global__ void __launch_bounds__(ADJ2_EX *ADJ2_EY, 2)
+    adjoint2_tma_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_pa,
+                        const __grid_constant__ CUtensorMap map_pb, Adj2Args a)
+{
+    static_assert(NS == ADJ2T_NS, "two stages");
+    static_assert(ADJ2_LAG == 1, "the staged kernel runs step B one plane behind step A");
+    static_assert(LBM_ADJ2M_EY == ADJ2_EY, "the staged kernel uses the 32 x 8 tiles");
+    extern __shared__ __align__(128) unsigned char adj2t_raw[];
+    float *stages = reinterpret_cast<float *>(adj2t_raw);
+    float *slots = stages + ADJ2T_NS * ADJ2T_STAGE;
+    constexpr int EY = ADJ2_EY, TY = EY - 2;
+    constexpr int PL = ADJ2_EX * EY;
+    uint64_t *full = reinterpret_cast<uint64_t *>(slots + ADJ2_SLOTS * PL);
+    constexpr Adj2Layout LAY = adj2_layout();
+    constexpr int DP = 2, D0 = 3, DM = 4;  // plane slots of a population with ez = +1, 0, -1
+    const int dim = a.dim;
+    const unsigned plane = (unsigned)dim * (unsigned)dim;
+    const int lx = (int)threadIdx.x % ADJ2_EX, ly = (int)threadIdx.x / ADJ2_EX;
+    int t = (int)blockIdx.x;
+    const int tx = t % a.ntx;
+    t /= a.ntx;
+    const int ty = t % a.nty, tz = t / a.nty;
+    const int xi0 = 1 + tx * ADJ2_TX, yi0 = 1 + ty * TY, zi0 = 1 + tz * a.zc;
+    const int zi1 = min(zi0 + a.zc, dim - 1);  // owned planes [zi0, zi1)
+    const int x = xi0 - 1 + lx, y = yi0 - 1 + ly;
+    const bool in_dom = x < dim && y < dim;
+    const bool owned = lx >= 1 && lx <= ADJ2_TX && ly >= 1 && ly <= TY && x <= dim - 2 && y <= dim - 2;
+    const bool ext_fluid = xi0 - 1 >= 2 && xi0 + ADJ2_EX - 2 <= dim - 3 && yi0 - 1 >= 2 && yi0 + EY - 2 <= dim - 3;
+    const bool own_fluid = xi0 >= 2 && xi0 + ADJ2_TX - 1 <= dim - 3 && yi0 >= 2 && yi0 + TY - 1 <= dim - 3;
+    // box origin in x (16-byte aligned; -4 for the first tile column) and the
+    // box column of this thread's site
+    const int xs = ((xi0 - 2) >> 2) * 4;
+    const int col0 = lx + (xi0 - 1 - xs);
+    const int ybox = yi0 - 1;  // box row 0 = the ext tile's first row
+    const float *lid = static_cast<const float *>(a.lid);
+    const float omega = a.omega;
+    float dl = 0.f;
+    const unsigned col = (unsigned)y * (unsigned)dim + (unsigned)x;
+    // register-held populations of a_k (0: planes p, p - 1; 5: p .. p - 2);
+    // population 6 of step B is the current step A's
+    float h0[2] = {0.f, 0.f}, h5[3] = {0.f, 0.f, 0.f};
+
+    const int p0 = zi0 - 1;
+    const int np = zi1 - p0 + 1;  // step A at planes p0 .. zi1, step B one behind
+    // stage j (plane p0 + j) into ring slot j % 2; thread 0 only (warp 0 has
+    // no step-B sites, so the issue stays off the block's critical path)
+    auto issue = [&](int j) {
+        const int p = p0 + j;
+        float *st = stages + (j & 1) * ADJ2T_STAGE;
+        uint64_t *bar = &full[j & 1];
+        mbar_expect_tx(bar, (uint32_t)(ADJ2T_STAGE * sizeof(float)));
+#pragma unroll
+        for (int i = 0; i < Q; ++i) tma_load_4d(st + i * ADJ2T_BOX, &map_a, xs, ybox + ey_of(i), p + ez_of(i), i, bar);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) tma_load_4d(st + (Q + c) * ADJ2T_BOX, &map_pa, xs, ybox, p, c, bar);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) tma_load_4d(st + (Q + 3 + c) * ADJ2T_BOX, &map_pb, xs, ybox, p - 1, c, bar);
+    };
+    if (threadIdx.x == 0) {
+        mbar_init(&full[0], 1);
+        mbar_init(&full[1], 1);
+        mbar_fence_init();
+        for (int k = 0; k < min(ADJ2T_NS, np); ++k) issue(k);
+    }
+    __syncthreads();
+
+    int j = 0;
+    bool err = false;
+    for (; j < np; ++j) {
+        const int p = p0 + j;
+        const float *st = stages + (j & 1) * ADJ2T_STAGE;
+        const bool bad = !mbar_wait_bounded(&full[j & 1], (uint32_t)(j >> 1) & 1u, kWaitLimit);
+        h5[2] = h5[1];
+        h5[1] = h5[0];
+        h0[1] = h0[0];
+        // ---- step A: a_k at (x, y, p) of the ext tile (p <= zi1 always)
+        {
+            float b[Q];
+            const unsigned site = (unsigned)p * plane + col;
+            uint8_t b8 = M_WALL;
+            if (in_dom) b8 = (ext_fluid && p >= 2 && p <= dim - 3) ? (uint8_t)0 : __ldg(a.map + site);
+            if (b8 & M_WALL) {
+#pragma unroll
+                for (int i = 0; i < Q; ++i) b[i] = 0.f;
+            } else {
+                const float *row = st + ly * ADJ2T_BW + col0;
+#pragma unroll
+                for (int i = 0; i < Q; ++i) b[i] = row[i * ADJ2T_BOX + ex_of(i)];
+                float l = 0.f;
+                const float lidv = (b8 & M_FRONT) ? lid[col] : 0.f;
+                adjoint_site_macro<float>(b, b8, row[Q * ADJ2T_BOX], row[(Q + 1) * ADJ2T_BOX],
+                                          row[(Q + 2) * ADJ2T_BOX], lidv, omega, l);
+                if (owned && p >= zi0 && p < zi1) dl += l;
+            }
+            const int mp = p % DP, m0 = p % D0, mm = p % DM;
+#pragma unroll
+            for (int i = 0; i < Q; ++i) {
+                if (adj2_in_regs(i)) continue;
+                const int slot = LAY.base[i] + (ez_of(i) == 1 ? mp : (ez_of(i) == 0 ? m0 : mm));
+                slots[slot * PL + threadIdx.x] = b[i];
+            }
+            h0[0] = b[0];
+            h5[0] = b[5];
+            const float b6 = b[6];
+            // ---- step B's inputs: its points (from this stage) and its map
+            const int q = p - 1;
+            const bool do_b = owned && q >= zi0 && q < zi1;
+            const unsigned site_b = (unsigned)q * plane + col;
+            float mb[3];
+            uint8_t b8b = 0;
+            {
+                const float *row = st + ly * ADJ2T_BW + col0;
+                mb[0] = row[(Q + 3) * ADJ2T_BOX];
+                mb[1] = row[(Q + 4) * ADJ2T_BOX];
+                mb[2] = row[(Q + 5) * ADJ2T_BOX];
+            }
+            if (do_b) b8b = (own_fluid && q >= 2 && q <= dim - 3) ? (uint8_t)0 : __ldg(a.map + site_b);
+            // every thread has read stage j and written its plane slots
+            if (__syncthreads_or(bad)) {
+                err = true;
+                break;
+            }
+            if (threadIdx.x == 0 && j + ADJ2T_NS < np) issue(j + ADJ2T_NS);
+            // ---- step B: a_{k-1} at (x, y, q) of the owned tile
+            if (do_b) {
+                const int mq = (q + 1) % DP, m0q = q % D0, mmq = (q + DM - 1) % DM;
+                float bb[Q];
+#pragma unroll
+                for (int i = 0; i < Q; ++i) {
+                    if (adj2_in_regs(i)) continue;
+                    const int slot = LAY.base[i] + (ez_of(i) == 1 ? mq : (ez_of(i) == 0 ? m0q : mmq));
+                    bb[i] = slots[slot * PL + (ly + ey_of(i)) * ADJ2_EX + (lx + ex_of(i))];
+                }
+                bb[0] = h0[1];
+                bb[5] = h5[2];
+                bb[6] = b6;
+                float l = 0.f;
+                const float lidv = (b8b & M_FRONT) ? lid[col] : 0.f;
+                adjoint_site_macro<float>(bb, b8b, mb[0], mb[1], mb[2], lidv, omega, l);
+                dl += l;
+#pragma unroll
+                for (int i = 0; i < Q; ++i) a.aout[site_b + a.off_own[i]] = bb[i];
+            }
+        }
+    }
+    if (err) {
+        if (threadIdx.x == 0) {
+            atomicOr(a.status, 2);
+            // drain what was issued and not consumed (stages j .. j + 1; bounded)
+            for (int k = j; k < min(j + ADJ2T_NS, np); ++k)
+                mbar_wait_bounded(&full[k & 1], (uint32_t)(k >> 1) & 1u, kWaitLimit);
+        }
+        return;
+    }
+    // one MOVING site per column, in one chunk: a single writer per column
+    if (owned && zi0 <= dim - 2 && dim - 2 < zi1) a.grad_lid[col] += (double)dl;
 }
 
 // Seed of the backward sweep: a_T = dJ/dR_T for the mid-plane loss

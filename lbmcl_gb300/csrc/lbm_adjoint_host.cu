@@ -19,7 +19,10 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <vector>
+
+#include <cudaTypedefs.h>
 
 #include "lbm.h"
 #include "lbm_adjoint.cuh"
@@ -161,11 +164,62 @@ cudaError_t set_adjoint2_smem()
     return e;
 }
 
+// ---- TMA-staged stored-point two-step kernel
+// cuTensorMapEncodeTiled, looked up once through the runtime (the library
+// does not link against the driver library)
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    });
+    return fn;
+}
+
+// A (dim, dim, dim, planes) float tensor at base with 40 x 8 x 1 x 1 boxes;
+// coordinates outside it read as zeros.  Needs dim % 4 == 0 (row strides of
+// 16-byte multiples) and a 16-byte aligned base.
+bool adj2t_map(CUtensorMap *m, const void *base, int dim, int planes)
+{
+    const PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+    if (!enc) return false;
+    const cuuint64_t d = (cuuint64_t)dim;
+    const cuuint64_t gdim[4] = {d, d, d, (cuuint64_t)planes};
+    const cuuint64_t gstride[3] = {d * 4, d * d * 4, d * d * d * 4};
+    const cuuint32_t box[4] = {(cuuint32_t)lbm::ADJ2T_BW, (cuuint32_t)lbm::ADJ2_EY, 1, 1};
+    const cuuint32_t estride[4] = {1, 1, 1, 1};
+    return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, const_cast<void *>(base), gdim, gstride, box, estride,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// The staged kernel runs the stored-point pairs of steps when asked for
+// (lbm_config.adjoint_kernel = LBM_KERNEL_STAGED); it needs dim % 4 == 0
+// (always true of FP32 / FP16 / BF16 handles) and the driver's tensor maps.
+// Not the default: at two blocks per SM (its shared memory) it measured 4%
+// slower per backward iteration than the per-thread-load kernel at four
+// (256^3 FP16: 0.651 against 0.625 ms), bound by its per-plane barrier.
+bool adj2_staged(const lbm_t *h)
+{
+    return h->cfg.adjoint_kernel == LBM_KERNEL_STAGED && h->dim % 4 == 0 && tensor_map_encoder() != nullptr;
+}
+
 // The two-step kernels' shared-memory size, set at the start of every
 // backward sweep (outside any graph capture): the attribute belongs to the
 // current device's context, and handles may live on different devices.
 cudaError_t prepare_adjoint2(const lbm_t *h)
 {
+    if (h->prec != LBM_FP64) {
+        const cudaError_t e = cudaFuncSetAttribute(lbm::adjoint2_tma_kernel<lbm::ADJ2T_NS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                   (int)lbm::adj2t_smem_bytes());
+        if (e != cudaSuccess) return e;
+    }
     switch (h->prec) {
     case LBM_FP32: return set_adjoint2_smem<float>();
     case LBM_FP16: return set_adjoint2_smem<__half>();
@@ -201,6 +255,15 @@ cudaError_t adjoint_two_steps(const lbm_t *h, const void *fwd_a, const void *fwd
     a.omega = (float)h->inv_tau;
     a.status = h->status;
     const unsigned grid = adj2_grid(h, a.ntx, a.nty, macro);
+    if (macro && adj2_staged(h)) {
+        CUtensorMap ma, mpa, mpb;
+        if (!adj2t_map(&ma, ain, h->dim, lbm::Q) || !adj2t_map(&mpa, fwd_a, h->dim, 3) ||
+            !adj2t_map(&mpb, fwd_b, h->dim, 3))
+            return cudaErrorInvalidValue;
+        lbm::adjoint2_tma_kernel<lbm::ADJ2T_NS><<<grid, lbm::ADJ2_EX * lbm::ADJ2_EY, lbm::adj2t_smem_bytes(), h->stream>>>(ma, mpa,
+                                                                                                           mpb, a);
+        return cudaGetLastError();
+    }
     switch (h->prec) {
     case LBM_FP32: return macro ? run_adjoint2<float, true>(a, grid, h->stream) : run_adjoint2<float, false>(a, grid, h->stream);
     case LBM_FP16:

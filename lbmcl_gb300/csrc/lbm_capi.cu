@@ -407,6 +407,10 @@ int lbm_init(lbm_t **out, const lbm_config *c)
         return fail(LBM_EINVAL, "lbm_init: adjoint_fp64 %d must be 0 or 1", c->adjoint_fp64);
     if (c->adjoint_full_states < 0 || c->adjoint_full_states > 1)
         return fail(LBM_EINVAL, "lbm_init: adjoint_full_states %d must be 0 or 1", c->adjoint_full_states);
+    if (c->adjoint_kernel != LBM_KERNEL_AUTO && c->adjoint_kernel != LBM_KERNEL_DIRECT &&
+        c->adjoint_kernel != LBM_KERNEL_STAGED)
+        return fail(LBM_EINVAL, "lbm_init: adjoint_kernel %d must be 0, LBM_KERNEL_DIRECT or LBM_KERNEL_STAGED",
+                    c->adjoint_kernel);
     if (c->order < LBM_ORDER_REFERENCE || c->order > LBM_ORDER_SAILFISH)
         return fail(LBM_EINVAL, "lbm_init: unknown summation order %d", c->order);
     if (c->order == LBM_ORDER_SAILFISH && c->precision != LBM_FP32 && c->precision != LBM_FP64)

@@ -29,11 +29,13 @@ def main(argv=None) -> int:
     ap.add_argument("--adjoint", default="", help="T,c: also run an adjoint forward/backward of T iterations, "
                                                   "checkpoint every c")
     ap.add_argument("--tau", action="store_true", help="the adjoint also forms dJ/dtau (full-state segments)")
+    ap.add_argument("--adjoint-kernel", default="auto", choices=["auto", "direct", "staged"],
+                    help="two-step adjoint of the stored-point sweep: per-thread loads or TMA-staged planes")
     a = ap.parse_args(argv)
     with capi.Lattice(a.dim, a.viscosity, a.velocity, precision=a.precision, stride=0, seed=a.seed,
                       noise_sigma=a.noise, block_threads=a.block, profile_steps=True, kernel=a.kernel,
                       stages=a.stages, adjoint_steps=a.adjoint_steps,
-                      adjoint_max_states=a.adjoint_max_states) as L:
+                      adjoint_max_states=a.adjoint_max_states, adjoint_kernel=a.adjoint_kernel) as L:
         t0 = time.perf_counter()
         L.step(a.steps, every=a.every)
         L.sync()

@@ -170,3 +170,27 @@ def test_fp32_adjoint_equals_fp64_adjoint_of_the_same_trajectory(capi, prec, wan
     assert np.linalg.norm(f32 - f64) <= 1e-5 * np.linalg.norm(f64)
     if want_tau:
         assert abs(t32 - t64) <= 1e-5 * abs(t64)
+
+
+@pytest.mark.parametrize("prec,dim,iters,every", [("fp32", 16, 23, 6), ("fp16", 40, 17, 17), ("bf16", 64, 12, 4),
+                                                  ("fp32", 100, 9, 9), ("fp16", 136, 7, 7), ("fp32", 68, 30, 10)])
+def test_staged_two_step_adjoint(capi, prec, dim, iters, every):
+    """The two-step stored-point adjoint with its planes staged by TMA, across
+    tile columns whose boxes start left of the lattice (x = -4) or run past
+    its end, several z-chunks and odd segments: bit for bit the initial
+    population gradient of one adjoint step per launch (the same arithmetic
+    per site; the lid gradient sums a column's terms in another order) and
+    within rounding of the two-step kernel that loads from HBM per thread."""
+    one = grads(capi, prec, dim, iters, every, False, adjoint_steps=1)
+    direct = grads(capi, prec, dim, iters, every, False, adjoint_steps=2, adjoint_kernel="direct")
+    staged = grads(capi, prec, dim, iters, every, False, adjoint_steps=2, adjoint_kernel="staged")
+    again = grads(capi, prec, dim, iters, every, False, adjoint_steps=2, adjoint_kernel="staged")
+    for r in (direct, staged, again):
+        assert r[0] == one[0] and r[1] is None
+    np.testing.assert_array_equal(staged[3], one[3])
+    np.testing.assert_array_equal(staged[2], again[2])
+    np.testing.assert_array_equal(staged[3], again[3])
+    for ref in (one, direct):
+        assert np.abs(staged[2] - ref[2]).max() <= 1e-6 * np.abs(ref[2]).max()
+        assert np.abs(staged[3] - ref[3]).max() <= 1e-6 * np.abs(ref[3]).max()
+    assert np.abs(staged[2]).max() > 0 and np.isfinite(staged[3]).all()
