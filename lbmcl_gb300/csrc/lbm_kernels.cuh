@@ -19,6 +19,8 @@
 
 #include <string.h>
 
+#include <type_traits>
+
 #include "lbm_device.cuh"
 #include "lbm_noise.cuh"
 
@@ -276,16 +278,10 @@ __device__ __forceinline__ void moments_dev(const float (&D)[Q], float inv_s, fl
     uz = __fmul_rn(jz, kk);
 }
 
-// FLUID site in deviation form.
-template <bool COLLIDE>
-__device__ __forceinline__ void fluid_dev(float (&D)[Q], const DevK &K, SiteOut &o)
+// The BGK update of fluid_dev for one site from its moments.
+__device__ __forceinline__ void relax_dev(float (&D)[Q], float drho, float rho, float ux, float uy, float uz,
+                                          const DevK &K)
 {
-    float drho, rho, ux, uy, uz;
-    moments_dev(D, K.inv_s, drho, rho, ux, uy, uz);
-    o.macro = true;
-    o.bad = !(rho > 0.0f);
-    o.r = rho; o.ux = ux; o.uy = uy; o.uz = uz;
-    if (!COLLIDE) return;
     const float c15 = __fmul_rn(1.5f, __fmaf_rn(ux, ux, __fmaf_rn(uy, uy, __fmul_rn(uz, uz))));
     D[0] = __fmaf_rn(K.keep, D[0], __fmul_rn(K.k[0], __fmaf_rn(rho, -c15, drho)));
     relax_pair_dev(D[1], D[3], ux, 1, rho, drho, c15, K);
@@ -297,6 +293,95 @@ __device__ __forceinline__ void fluid_dev(float (&D)[Q], const DevK &K, SiteOut 
     relax_pair_dev(D[12], D[18], __fsub_rn(uy, uz), 2, rho, drho, c15, K);
     relax_pair_dev(D[15], D[13], __fadd_rn(ux, uz), 2, rho, drho, c15, K);
     relax_pair_dev(D[16], D[14], __fadd_rn(uy, uz), 2, rho, drho, c15, K);
+}
+
+// FLUID site in deviation form.
+template <bool COLLIDE>
+__device__ __forceinline__ void fluid_dev(float (&D)[Q], const DevK &K, SiteOut &o)
+{
+    float drho, rho, ux, uy, uz;
+    moments_dev(D, K.inv_s, drho, rho, ux, uy, uz);
+    o.macro = true;
+    o.bad = !(rho > 0.0f);
+    o.r = rho; o.ux = ux; o.uy = uy; o.uz = uz;
+    if (COLLIDE) relax_dev(D, drho, rho, ux, uy, uz, K);
+}
+
+// Two FLUID sites at once on packed FP32 pairs (lane .x one site, .y the
+// other): the operations of moments_dev / fluid_dev in the same order and
+// rounding (add/mul/fma .rn on f32x2), so each lane's result is bit for bit
+// the scalar one, in fewer arithmetic instructions.  RELAX2: the BGK update
+// packed too (its constants then live as register pairs), else per lane with
+// the scalar relax_pair_dev.
+__device__ __forceinline__ float2 f2_(float v) { return make_float2(v, v); }
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a, neg2(b)); }  // exact: a + (-b)
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+
+__device__ __forceinline__ void relax_pair_dev2(float2 &dp, float2 &dm, float2 a, int c, float2 rho, float2 drho,
+                                                float2 c15, const DevK &K)
+{
+    const float2 p = fma2(mul2(f2_(4.5f), a), a, neg2(c15));
+    const float2 X = fma2(rho, p, drho);
+    const float2 lin = mul2(mul2(f2_(K.k3[c]), rho), a);
+    dp = fma2(f2_(K.keep), dp, fma2(f2_(K.k[c]), X, lin));
+    dm = fma2(f2_(K.keep), dm, fma2(f2_(K.k[c]), X, neg2(lin)));
+}
+
+template <bool COLLIDE, bool RELAX2>
+__device__ __forceinline__ void fluid_dev2(float2 (&D)[Q], const DevK &K, SiteOut &o0, SiteOut &o1)
+{
+    const float2 s13 = add2(D[1], D[3]), d13 = sub2(D[1], D[3]);
+    const float2 s24 = add2(D[2], D[4]), d24 = sub2(D[2], D[4]);
+    const float2 s56 = add2(D[5], D[6]), d65 = sub2(D[6], D[5]);
+    const float2 s79 = add2(D[7], D[9]), d79 = sub2(D[7], D[9]);
+    const float2 s810 = add2(D[8], D[10]), d810 = sub2(D[8], D[10]);
+    const float2 s1117 = add2(D[11], D[17]), d1117 = sub2(D[11], D[17]);
+    const float2 s1218 = add2(D[12], D[18]), d1218 = sub2(D[12], D[18]);
+    const float2 s1315 = add2(D[13], D[15]), d1513 = sub2(D[15], D[13]);
+    const float2 s1416 = add2(D[14], D[16]), d1614 = sub2(D[16], D[14]);
+    const float2 sd = add2(add2(D[0], s1416), add2(add2(add2(s13, s24), add2(s56, s79)),
+                                                   add2(add2(s810, s1117), add2(s1218, s1315))));
+    const float2 jx = add2(sub2(add2(d13, d79), d810), add2(d1117, d1513));
+    const float2 jy = add2(add2(add2(d24, d79), d810), add2(d1218, d1614));
+    const float2 jz = add2(sub2(sub2(d65, d1117), d1218), add2(d1513, d1614));
+    const float2 drho = mul2(sd, f2_(K.inv_s));
+    const float2 rho = add2(f2_(1.0f), drho);
+    const float2 kk = mul2(f2_(K.inv_s), make_float2(__fdividef(1.0f, rho.x), __fdividef(1.0f, rho.y)));
+    const float2 ux = mul2(jx, kk), uy = mul2(jy, kk), uz = mul2(jz, kk);
+    o0.macro = o1.macro = true;
+    o0.bad = !(rho.x > 0.0f);
+    o1.bad = !(rho.y > 0.0f);
+    o0.r = rho.x; o0.ux = ux.x; o0.uy = uy.x; o0.uz = uz.x;
+    o1.r = rho.y; o1.ux = ux.y; o1.uy = uy.y; o1.uz = uz.y;
+    if (!COLLIDE) return;
+    if constexpr (RELAX2) {
+        const float2 c15 = mul2(f2_(1.5f), fma2(ux, ux, fma2(uy, uy, mul2(uz, uz))));
+        D[0] = fma2(f2_(K.keep), D[0], mul2(f2_(K.k[0]), fma2(rho, neg2(c15), drho)));
+        relax_pair_dev2(D[1], D[3], ux, 1, rho, drho, c15, K);
+        relax_pair_dev2(D[2], D[4], uy, 1, rho, drho, c15, K);
+        relax_pair_dev2(D[6], D[5], uz, 1, rho, drho, c15, K);
+        relax_pair_dev2(D[7], D[9], add2(ux, uy), 2, rho, drho, c15, K);
+        relax_pair_dev2(D[8], D[10], sub2(uy, ux), 2, rho, drho, c15, K);
+        relax_pair_dev2(D[11], D[17], sub2(ux, uz), 2, rho, drho, c15, K);
+        relax_pair_dev2(D[12], D[18], sub2(uy, uz), 2, rho, drho, c15, K);
+        relax_pair_dev2(D[15], D[13], add2(ux, uz), 2, rho, drho, c15, K);
+        relax_pair_dev2(D[16], D[14], add2(uy, uz), 2, rho, drho, c15, K);
+    } else {
+        float L[Q];
+#pragma unroll
+        for (int i = 0; i < Q; ++i) L[i] = D[i].x;
+        relax_dev(L, drho.x, rho.x, ux.x, uy.x, uz.x, K);
+#pragma unroll
+        for (int i = 0; i < Q; ++i) D[i].x = L[i];
+#pragma unroll
+        for (int i = 0; i < Q; ++i) L[i] = D[i].y;
+        relax_dev(L, drho.y, rho.y, ux.y, uy.y, uz.y, K);
+#pragma unroll
+        for (int i = 0; i < Q; ++i) D[i].y = L[i];
+    }
 }
 
 // Any site in deviation form (walls, faces, corners, lid, fluid).
@@ -503,6 +588,22 @@ __device__ __forceinline__ void update_general(S (&fs)[Q][V], typename MapWord<V
     if (bad) atomicOr(a.status, 1);
 }
 
+// Instruction form of the all-FLUID pairs of the 16-bit kernels (the same
+// bits either way): 0 = two scalar site updates, 1 = packed FP32x2 moments
+// and scalar BGK updates, 2 = packed throughout.  Chosen per storage type by
+// measurement at 512^3 (the packed forms change the register allocation at
+// the 168-register cap, which decides).
+#ifndef LBM_DEV16_FORM_F16
+#define LBM_DEV16_FORM_F16 0
+#endif
+#ifndef LBM_DEV16_FORM_BF16
+#define LBM_DEV16_FORM_BF16 2
+#endif
+template <class S> __host__ __device__ constexpr int dev16_form()
+{
+    return sizeof(S) != 2 ? 0 : (std::is_same<S, __half>::value ? LBM_DEV16_FORM_F16 : LBM_DEV16_FORM_BF16);
+}
+
 // Update the V sites x0..x0+V-1 of row (y, z) in place: fs holds their pulled
 // populations on entry and their post-collision populations on exit.  Stores
 // rho / u (MODE_STEP_MACRO) or accumulates the reduction sums (MODE_REDUCE).
@@ -553,18 +654,30 @@ __device__ __forceinline__ void update_vector(S (&fs)[Q][V], typename MapWord<V>
             // two sites per step so the output converts as packed pairs
 #pragma unroll
             for (int k = 0; k < V; k += 2) {
-                float D0[Q], D1[Q];
-#pragma unroll
-                for (int i = 0; i < Q; ++i) {
-                    D0[i] = Dev16<S>::to_f(fs[i][k]);
-                    D1[i] = Dev16<S>::to_f(fs[i][k + 1]);
-                }
                 SiteOut o0, o1;
-                fluid_dev<MODE != MODE_REDUCE>(D0, K, o0);
-                fluid_dev<MODE != MODE_REDUCE>(D1, K, o1);
-                if (MODE != MODE_REDUCE) {
+                if constexpr (dev16_form<S>() == 0) {
+                    float D0[Q], D1[Q];
 #pragma unroll
-                    for (int i = 0; i < Q; ++i) Dev16<S>::from_f2(D0[i], D1[i], fs[i][k], fs[i][k + 1]);
+                    for (int i = 0; i < Q; ++i) {
+                        D0[i] = Dev16<S>::to_f(fs[i][k]);
+                        D1[i] = Dev16<S>::to_f(fs[i][k + 1]);
+                    }
+                    fluid_dev<MODE != MODE_REDUCE>(D0, K, o0);
+                    fluid_dev<MODE != MODE_REDUCE>(D1, K, o1);
+                    if (MODE != MODE_REDUCE) {
+#pragma unroll
+                        for (int i = 0; i < Q; ++i) Dev16<S>::from_f2(D0[i], D1[i], fs[i][k], fs[i][k + 1]);
+                    }
+                } else {
+                    float2 D[Q];
+#pragma unroll
+                    for (int i = 0; i < Q; ++i)
+                        D[i] = make_float2(Dev16<S>::to_f(fs[i][k]), Dev16<S>::to_f(fs[i][k + 1]));
+                    fluid_dev2<MODE != MODE_REDUCE, dev16_form<S>() == 2>(D, K, o0, o1);
+                    if (MODE != MODE_REDUCE) {
+#pragma unroll
+                        for (int i = 0; i < Q; ++i) Dev16<S>::from_f2(D[i].x, D[i].y, fs[i][k], fs[i][k + 1]);
+                    }
                 }
                 // in an interior row, x in [2, dim-3] is FLUID; the row ends are walls / faces
                 const bool f0 = !FLUID_ONLY || (unsigned)(x0 + k - 2) <= (unsigned)(dim - 5);
