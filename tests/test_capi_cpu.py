@@ -56,6 +56,8 @@ def _init(libonly, **kw):
     (dict(graph_iterations=512), "graph_iterations"),
     (dict(order=2), "summation order"),
     (dict(order=1, precision=3), "Sailfish"),   # FP16 storage: its own deviation sums
+    (dict(adjoint_kernel=3), "adjoint_kernel"),  # only auto, direct or staged
+    (dict(adjoint_kernel=-1), "adjoint_kernel"),
 ])
 def test_init_rejects_bad_arguments(libonly, kw, frag):
     rc, msg = _init(libonly, **kw)
