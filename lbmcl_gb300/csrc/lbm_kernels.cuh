@@ -1235,45 +1235,18 @@ __device__ __forceinline__ C lid_at(const InitArgs &a, int x, int y)
     return static_cast<const C *>(a.lid)[(size_t)y * a.dim + x];
 }
 
-// Grid: blockIdx.y = z-plane, x-blocks over the dim^2 sites of the plane
-// (32-bit index arithmetic inside a plane).
+// The population slots a site's initial state writes (all but those that
+// noise_kernel owns): P_{-1} slots pulled into the site (or, in A-form, its
+// own R_0 slots).
 template <class S>
-__global__ void init_kernel(InitArgs a)
+__device__ __forceinline__ void init_site_pops(const InitArgs &a, int x, int y, int z, size_t id, uint8_t b)
 {
     using C = typename Compute<S>::type;
     const int dim = a.dim;
-    const unsigned pi = blockIdx.x * blockDim.x + threadIdx.x;
-    if (pi >= (unsigned)dim * (unsigned)dim) return;
-    const int x = (int)(pi % (unsigned)dim), y = (int)(pi / (unsigned)dim), z = (int)blockIdx.y;
-    const size_t id = (size_t)z * dim * dim + pi;
-    const uint8_t b = pack_cell(dim, x, y, z);
-    a.map[id] = b;
-    const bool store = (b == 0) || (b == M_FRONT);
-    C *rho = static_cast<C *>(a.rho);
-    C *u = static_cast<C *>(a.u);
     const C qn = nan_of<C>();
-    rho[id] = store ? (C)1 : qn;
-    u[id] = store ? ((b & M_FRONT) ? lid_at<C>(a, x, y) : (C)0) : qn;
-    u[a.n + id] = store ? (C)0 : qn;
-    u[2 * a.n + id] = store ? (C)0 : qn;
-
     S *f = static_cast<S *>(a.f);
     const Weights<C> W = make_weights<C>();
-    // With noise, noise_kernel writes every slot whose value belongs to a
-    // FLUID site (the slots streaming into it, or its own in A-form); this
-    // kernel writes the others.
     const bool noisy = a.noise_sigma != 0.0;
-    if (x >= 3 && y >= 3 && z >= 3 && x <= dim - 4 && y <= dim - 4 && z <= dim - 4) {
-        // the site and all its neighbours are FLUID: the rest state
-        if (!noisy) {
-#pragma unroll
-            for (int i = 0; i < Q; ++i) {
-                if constexpr (is_dev16<S>()) f[(size_t)i * a.n + id] = Dev16<S>::from_f(0.0f);
-                else f[(size_t)i * a.n + id] = (S)W.w[wclass_of(i)];
-            }
-        }
-        return;
-    }
 #pragma unroll
     for (int i = 0; i < Q; ++i) {
         C val = qn;  // walls hold NaN (kernels.cl:312, 316)
@@ -1319,6 +1292,102 @@ __global__ void init_kernel(InitArgs a)
         }
     }
 }
+
+// Four values of type T at p (4-element aligned) with one or two vector
+// stores.
+template <class T> __device__ __forceinline__ void store4(T *p, const T (&v)[4])
+{
+    if constexpr (sizeof(T) == 8) {
+        reinterpret_cast<double2 *>(p)[0] = make_double2(v[0], v[1]);
+        reinterpret_cast<double2 *>(p)[1] = make_double2(v[2], v[3]);
+    } else if constexpr (sizeof(T) == 4) {
+        *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
+    } else {
+        uint2 r;
+        memcpy(&r, v, 8);
+        *reinterpret_cast<uint2 *>(p) = r;
+    }
+}
+
+// Grid: blockIdx.y = z-plane, x-blocks over the plane's dim^2 / 4 groups of
+// four consecutive x-sites (dim % 4 == 0; 32-bit index arithmetic inside a
+// plane).  Each thread writes its four sites' map bytes, rho and u with one
+// vector store per field; the population slots of sites whose neighbours
+// are all FLUID take a branch-free path (nothing with noise, the rest state
+// without), the others init_site_pops.
+template <class S>
+__global__ void init_kernel(InitArgs a)
+{
+    using C = typename Compute<S>::type;
+    const int dim = a.dim;
+    const unsigned nq = (unsigned)dim / 4u;
+    const unsigned pi = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pi >= nq * (unsigned)dim) return;
+    const int y = (int)(pi / nq), x0 = 4 * (int)(pi - (unsigned)y * nq), z = (int)blockIdx.y;
+    const size_t id0 = (size_t)z * dim * dim + (size_t)y * dim + (size_t)x0;
+    uint8_t b[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) b[k] = pack_cell(dim, x0 + k, y, z);
+    uint32_t mw;
+    memcpy(&mw, b, 4);
+    *reinterpret_cast<uint32_t *>(a.map + id0) = mw;
+    const C qn = nan_of<C>();
+    C r[4], ux[4], u0[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const bool store = (b[k] == 0) || (b[k] == M_FRONT);
+        r[k] = store ? (C)1 : qn;
+        ux[k] = store ? ((b[k] & M_FRONT) ? lid_at<C>(a, x0 + k, y) : (C)0) : qn;
+        u0[k] = store ? (C)0 : qn;
+    }
+    C *u = static_cast<C *>(a.u);
+    store4<C>(static_cast<C *>(a.rho) + id0, r);
+    store4<C>(u + id0, ux);
+    store4<C>(u + a.n + id0, u0);
+    store4<C>(u + 2 * a.n + id0, u0);
+
+    // With noise, noise_kernel writes every slot whose value belongs to a
+    // FLUID site (the slots streaming into it, or its own in A-form); this
+    // kernel writes the others.
+    const bool noisy = a.noise_sigma != 0.0;
+    const bool bulk = y >= 3 && z >= 3 && y <= dim - 4 && z <= dim - 4;
+    if (bulk && x0 >= 3 && x0 + 3 <= dim - 4) {
+        // every site and all its neighbours are FLUID: the rest state
+        if (!noisy) {
+            S *f = static_cast<S *>(a.f);
+            const Weights<C> W = make_weights<C>();
+#pragma unroll
+            for (int i = 0; i < Q; ++i) {
+                S v[4];
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    if constexpr (is_dev16<S>()) v[k] = Dev16<S>::from_f(0.0f);
+                    else v[k] = (S)W.w[wclass_of(i)];
+                }
+                store4<S>(f + (size_t)i * a.n + id0, v);
+            }
+        }
+        return;
+    }
+#pragma unroll 1
+    for (int k = 0; k < 4; ++k) {
+        const int x = x0 + k;
+        if (bulk && x >= 3 && x <= dim - 4) {
+            if (!noisy) {
+                S *f = static_cast<S *>(a.f);
+                const Weights<C> W = make_weights<C>();
+#pragma unroll
+                for (int i = 0; i < Q; ++i) {
+                    if constexpr (is_dev16<S>()) f[(size_t)i * a.n + id0 + k] = Dev16<S>::from_f(0.0f);
+                    else f[(size_t)i * a.n + id0 + k] = (S)W.w[wclass_of(i)];
+                }
+            }
+            continue;
+        }
+        init_site_pops<S>(a, x, y, z, id0 + k, b[k]);
+    }
+}
+
 
 // Seeded N(0, sigma^2) noise on the initial populations of the FLUID sites
 // (x, y, z in [2, dim-3]), run after init_kernel: the thread of FLUID site t

@@ -142,7 +142,8 @@ const void *LBM_CAT(staged_kernel_ptr_, LBM_SFX)(int mode)
 cudaError_t LBM_CAT(launch_init_, LBM_SFX)(const InitArgs &a, cudaStream_t s)
 {
     const unsigned block = 256;
-    const dim3 grid((unsigned)(((size_t)a.dim * a.dim + block - 1) / block), (unsigned)a.dim);
+    // four consecutive x-sites per thread (dim % 4 == 0)
+    const dim3 grid((unsigned)(((size_t)a.dim * a.dim / 4 + block - 1) / block), (unsigned)a.dim);
     init_kernel<LBM_S><<<grid, block, 0, s>>>(a);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess || a.noise_sigma == 0.0 || a.dim < 5) return e;
