@@ -144,6 +144,9 @@ void release(lbm_t *h)
         if (g) cudaGraphExecDestroy(g), g = nullptr;
     if (h->ev_first) cudaEventDestroy(h->ev_first);
     if (h->ev_last) cudaEventDestroy(h->ev_last);
+    if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+    if (h->ev_join) cudaEventDestroy(h->ev_join);
+    if (h->side) cudaStreamDestroy(h->side);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
 }
@@ -285,19 +288,49 @@ bool macro_within(int64_t it0, int G, int macro_every)
     return next <= it0 + G;
 }
 
+// One plain iteration of the direct / narrow variants inside a graph capture:
+// the face-row launch on the side stream, forked from and joined back into
+// the capture stream, so the graph runs it beside the interior-row launch
+// (they write disjoint rows of the output and read the same input).
+cudaError_t capture_split_iteration(const lbm_t *h, const lbm::StepArgs &a)
+{
+    cudaError_t e = cudaEventRecord(h->ev_fork, h->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(h->side, h->ev_fork, 0);
+    if (e != cudaSuccess) return e;
+    const int vb = h->kernel == LBM_KERNEL_NARROW ? 8 : 16;
+    switch (h->prec) {
+    case LBM_FP32: e = lbm::launch_split_f32(vb, a, h->block, h->stream, h->side); break;
+    case LBM_FP64: e = lbm::launch_split_f64(vb, a, h->block, h->stream, h->side); break;
+    case LBM_FP16: e = lbm::launch_split_f16(vb, a, h->block, h->stream, h->side); break;
+    default: e = lbm::launch_split_bf16(vb, a, h->block, h->stream, h->side); break;
+    }
+    // join even after a failed launch, so the capture can end
+    const cudaError_t ej = cudaEventRecord(h->ev_join, h->side);
+    const cudaError_t ew = ej == cudaSuccess ? cudaStreamWaitEvent(h->stream, h->ev_join, 0) : ej;
+    return e != cudaSuccess ? e : ew;
+}
+
 // Replay (capturing on first use) the graph of h->graph_iters plain
 // iterations that starts from buffer h->cur.  The kernels' arguments are
 // fixed per parity (the two buffers ping-pong), so two graphs cover every
-// call.
+// call.  With the direct / narrow kernels each iteration's face-row launch is
+// a branch beside its interior-row launch.
 cudaError_t replay_graph(lbm_t *h)
 {
     cudaGraphExec_t &exec = h->graph_exec[parity(h)];
     if (!exec) {
+        const bool split = h->kernel == LBM_KERNEL_DIRECT || h->kernel == LBM_KERNEL_NARROW;
+        if (split && !h->side) {
+            cudaError_t e = cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking);
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming);
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming);
+            if (e != cudaSuccess) return e;
+        }
         cudaError_t e = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal);
         if (e != cudaSuccess) return e;
         int cur = h->cur, ph = h->aa_phase;
         for (int k = 0; k < h->graph_iters && e == cudaSuccess; ++k) {
-            e = launch_pull(h, lbm::MODE_STEP, step_args(h, cur, ph));
+            e = split ? capture_split_iteration(h, step_args(h, cur, ph)) : launch_pull(h, lbm::MODE_STEP, step_args(h, cur, ph));
             if (is_aa(h)) ph ^= 1;
             else cur ^= 1;
         }

@@ -63,6 +63,10 @@ struct lbm_handle {
     double *red_out = nullptr;
     int *status = nullptr;
     cudaStream_t stream = nullptr;
+    // the iteration graphs' second branch (face-row launches beside the
+    // interior-row launches) and its fork / join events
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     cudaEvent_t ev_first = nullptr, ev_last = nullptr;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending;
     std::vector<cudaEvent_t> spare;

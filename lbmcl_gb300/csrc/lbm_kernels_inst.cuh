@@ -12,8 +12,11 @@ namespace lbm {
 // One iteration (or reduction pass) of the direct variant with VB-byte
 // vectors: the interior-row launch, then the face-row launch.  *nparts gets
 // the number of reduction partial slots the two launches use.
+// passes: bit 0 the interior-row launch, bit 1 the face-row launch (on
+// stream sf when given).
 template <int VB>
-static cudaError_t launch_direct(int mode, const StepArgs &a0, unsigned block, cudaStream_t s, unsigned *nparts)
+static cudaError_t launch_direct(int mode, const StepArgs &a0, unsigned block, cudaStream_t s, unsigned *nparts,
+                                 int passes = 3, cudaStream_t sf = nullptr)
 {
     constexpr int V = VB / (int)sizeof(LBM_S);
     StepArgs a = a0;
@@ -22,6 +25,8 @@ static cudaError_t launch_direct(int mode, const StepArgs &a0, unsigned block, c
     const unsigned gi = (unsigned)((m * m * (size_t)a.nvx + block - 1) / block);
     const unsigned gf = (unsigned)(((size_t)4 * (a.dim - 3) * (size_t)a.nvx + block - 1) / block);
     for (int pass = 0; pass < 2; ++pass) {
+        if (!(passes & (1 << pass))) continue;
+        if (pass == 1 && sf) s = sf;
         const unsigned grid = pass == 0 ? gi : gf;
         if (grid == 0) continue;
         a.partial_base = pass == 0 ? 0u : gi;
@@ -106,6 +111,18 @@ cudaError_t LBM_CAT(launch_pull_, LBM_SFX)(int mode, const StepArgs &a, unsigned
                                            unsigned *nparts)
 {
     return launch_direct<16>(mode, a, block, s, nparts);
+}
+
+// One plain iteration of the direct variant (VB = 16) or the narrow one
+// (VB = 8) with the face-row launch on stream sf, so that a graph captured
+// across the two streams runs the two launches side by side.
+cudaError_t LBM_CAT(launch_split_, LBM_SFX)(int vb, const StepArgs &a, unsigned block, cudaStream_t s, cudaStream_t sf)
+{
+    if (vb == 16) return launch_direct<16>(MODE_STEP, a, block, s, nullptr, 3, sf);
+    if constexpr (sizeof(LBM_S) < 8) {
+        if (vb == 8) return launch_direct<8>(MODE_STEP, a, block, s, nullptr, 3, sf);
+    }
+    return cudaErrorInvalidValue;
 }
 
 cudaError_t LBM_CAT(launch_narrow_, LBM_SFX)(int mode, const StepArgs &a, unsigned block, cudaStream_t s)
