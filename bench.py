@@ -288,7 +288,13 @@ def time_adjoint(capi, prec, device, with_tau=False):
         e1.record(stream)
         e1.synchronize()
         fwd_ms = e0.elapsed_time(e1) / 400
-    with capi.Lattice(dim, a["viscosity"], 0.0, precision=prec, lid=lid, stride=0, device=device) as L:
+    # lid-field control: the forward records the linearisation points of as
+    # many trailing segments as fit in device memory, and the backward skips
+    # recomputing those; with a tau gradient (full-state sweep) it would not
+    # use them
+    tail = -1 if with_tau else 0
+    with capi.Lattice(dim, a["viscosity"], 0.0, precision=prec, lid=lid, stride=0, device=device,
+                      adjoint_tail_segments=tail) as L:
         L.adjoint_set_loss(a["plane_y"], target)
         torch.cuda.synchronize(device)
         t0 = time.perf_counter()
@@ -303,7 +309,9 @@ def time_adjoint(capi, prec, device, with_tau=False):
     return {"dim": dim, "storage": prec, "adjoint": "fp32" if prec != "fp64" else "fp64", "iterations": T,
             "checkpoint_every": c,
             "control": "per-column lid 0.05 + N(0, 0.005)" + (" and tau" if with_tau else "") + ", mid-plane u_x loss",
-            "segments": "full states" if with_tau else "stored velocity / lid density per iteration",
+            "segments": "full states" if with_tau else ("stored velocity / lid density per iteration; the "
+                                                        "trailing segments that fit in device memory recorded by "
+                                                        "the forward, the others recomputed"),
             "forward_ms_per_iter": round(fwd_ms, 4),
             "checkpointed_forward_ms_per_iter": round(ckpt_ms, 4), "backward_ms_per_iter": round(bwd_ms, 4),
             "adjoint_over_forward": round(bwd_ms / fwd_ms, 3),

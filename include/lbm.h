@@ -131,6 +131,12 @@ typedef struct lbm_config {
                                   LBM_KERNEL_STAGED = each plane's inputs staged in shared
                                   memory by tiled TMA loads (dim % 4 == 0); the same
                                   per-site arithmetic                                      */
+    int adjoint_tail_segments; /* lbm_adjoint_forward also records the linearisation
+                                  points of its last checkpoint segments, so that a backward
+                                  sweep without a tau gradient does not recompute them:
+                                  0 = as many segments as fit in the device memory left
+                                  beyond what the sweep itself needs, n > 0 = at most n,
+                                  -1 = none; the gradients are the same bit for bit       */
 } lbm_config;
 
 /* Iteration kernel variants (same results, different data movement). */

@@ -29,10 +29,13 @@ class _CavityLoss(torch.autograd.Function):
     @staticmethod
     def forward(ctx, lid, tau, f0, opts):
         dim = opts["dim"]
+        # the forward records the last segments' linearisation points for a
+        # backward sweep without a tau gradient; with one it would not use them
         L = capi.Lattice(dim, velocity=0.0, precision=opts.get("precision", "fp32"),
                          stride=opts.get("stride"), lid=lid.detach().cpu().numpy().reshape(-1),
                          tau=float(tau), seed=opts.get("seed", 0), noise_sigma=opts.get("noise", 0.0),
-                         device=opts.get("device", 0))
+                         device=opts.get("device", 0),
+                         adjoint_tail_segments=-1 if ctx.needs_input_grad[1] else 0)
         if f0 is not None:
             L.load_f(f0.detach().cpu().numpy())
         L.adjoint_set_loss(opts["plane_y"], opts.get("target"))

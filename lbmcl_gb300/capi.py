@@ -55,6 +55,7 @@ class Config(C.Structure):
         ("adjoint_fp64", C.c_int),
         ("order", C.c_int),
         ("adjoint_kernel", C.c_int),
+        ("adjoint_tail_segments", C.c_int),
     ]
 
 
@@ -134,13 +135,17 @@ class Lattice:
     and u (FP32 / FP64).  adjoint_kernel: data movement of the FP32
     two-step adjoint in the stored-point sweep (0 = default, "direct" =
     per-thread loads, "staged" = TMA-staged planes; same results).
+    adjoint_tail_segments: checkpoint segments at the end of an adjoint
+    forward whose linearisation points it records, so a backward sweep
+    without a tau gradient skips recomputing them (0 = as many as fit, n = at
+    most n, -1 = none; same results).
     """
 
     def __init__(self, dim, viscosity=0.0089, velocity=0.05, precision="fp32", stride=None, lid=None,
                  seed=0, noise_sigma=0.0, tau=0.0, block_threads=0, max_device_bytes=0, device=0,
                  profile_steps=False, kernel=0, stages=0, adjoint_steps=0, adjoint_max_states=0,
                  graph_iterations=0, adjoint_full_states=False, adjoint_fp64=False, order="reference",
-                 adjoint_kernel=0):
+                 adjoint_kernel=0, adjoint_tail_segments=0):
         L = lib()
         c = default_config()
         c.dim = int(dim)
@@ -168,6 +173,7 @@ class Lattice:
         c.adjoint_fp64 = 1 if adjoint_fp64 else 0
         c.order = ORDERS[order] if isinstance(order, str) else int(order)
         c.adjoint_kernel = KERNELS[adjoint_kernel] if isinstance(adjoint_kernel, str) else int(adjoint_kernel)
+        c.adjoint_tail_segments = int(adjoint_tail_segments)
         self.cfg = c
         self.dim = int(dim)
         self.n = self.dim ** 3

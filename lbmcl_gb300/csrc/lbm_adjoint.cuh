@@ -799,7 +799,6 @@ __global__ void __launch_bounds__(ADJ2_EX *ADJ2_EY, 2)
 {
     static_assert(NS == ADJ2T_NS, "two stages");
     static_assert(ADJ2_LAG == 1, "the staged kernel runs step B one plane behind step A");
-    static_assert(LBM_ADJ2M_EY == ADJ2_EY, "the staged kernel uses the 32 x 8 tiles");
     extern __shared__ __align__(128) unsigned char adj2t_raw[];
     float *stages = reinterpret_cast<float *>(adj2t_raw);
     float *slots = stages + ADJ2T_NS * ADJ2T_STAGE;

@@ -207,7 +207,8 @@ bool adj2t_map(CUtensorMap *m, const void *base, int dim, int planes)
 // (256^3 FP16: 0.651 against 0.625 ms), bound by its per-plane barrier.
 bool adj2_staged(const lbm_t *h)
 {
-    return h->cfg.adjoint_kernel == LBM_KERNEL_STAGED && h->dim % 4 == 0 && tensor_map_encoder() != nullptr;
+    return h->cfg.adjoint_kernel == LBM_KERNEL_STAGED && lbm::adj2_ey<true>() == lbm::ADJ2_EY && h->dim % 4 == 0 &&
+           tensor_map_encoder() != nullptr;
 }
 
 // The two-step kernels' shared-memory size, set at the start of every
@@ -337,6 +338,22 @@ int alloc_tracked(lbm_t *h, void **p, size_t bytes)
     return LBM_OK;
 }
 
+// Device bytes the adjoint may still take: free memory less a margin for the
+// runtime and other users, within the handle's budget.
+size_t device_room(const lbm_t *h)
+{
+    size_t freeb = 0, totalb = 0;
+    if (cudaMemGetInfo(&freeb, &totalb) != cudaSuccess) return 0;
+    const size_t margin = ((size_t)1 << 30) + totalb / 50;
+    size_t r = freeb > margin ? freeb - margin : 0;
+    const size_t cap = h->cfg.max_device_bytes;
+    if (cap > 0) {
+        const size_t used = h->base_bytes + h->adj.bytes;
+        r = std::min(r, cap > used ? cap - used : (size_t)0);
+    }
+    return r;
+}
+
 void drop_segment_graphs(lbm_adjoint_state &s)
 {
     for (cudaGraphExec_t &g : s.seg_exec)
@@ -349,6 +366,16 @@ void free_tracked(lbm_t *h, void *p, size_t bytes)
     if (!p) return;
     cudaFree(p);
     h->adj.bytes -= bytes;
+}
+
+// the linearisation points the adjoint forward recorded for its last segments
+void free_tail_points(lbm_t *h)
+{
+    free_tracked(h, h->adj.tail_block, h->adj.tail_bytes);
+    h->adj.tail_block = nullptr;
+    h->adj.tail_bytes = 0;
+    h->adj.tpts.clear();
+    h->adj.tail_k0 = h->adj.iterations;
 }
 
 // The adjoint steps k = start + len - 1 .. start with Q_k (or, macro, its
@@ -517,9 +544,13 @@ void release_adjoint(lbm_t *h)
     for (void *p : s.ckpt) cudaFree(p);
     for (void *p : s.seg) cudaFree(p);
     for (void *p : s.mseg) cudaFree(p);
+    if (s.tail_block) cudaFree(s.tail_block);
+    s.tail_block = nullptr;
+    s.tail_bytes = 0;
     s.ckpt.clear();
     s.seg.clear();
     s.mseg.clear();
+    s.tpts.clear();
     for (void *&p : s.mtmp) {
         if (p) cudaFree(p);
         p = nullptr;
@@ -593,6 +624,7 @@ int lbm_adjoint_forward(lbm_t *h, int iterations, int checkpoint_every, double *
     for (void *p : s.seg) free_tracked(h, p, fbytes);
     s.ckpt.clear();
     s.seg.clear();
+    free_tail_points(h);
     drop_segment_graphs(s);
     s.ready = false;
     const int c = std::min(checkpoint_every, iterations);
@@ -607,12 +639,50 @@ int lbm_adjoint_forward(lbm_t *h, int iterations, int checkpoint_every, double *
     s.every = c;
     s.init_state = h->state_is_init;
 
+    // The last mt segments record their linearisation points here (the
+    // stored-point backward sweep then skips recomputing them): as many as
+    // fit in the device memory left once the sweep's own buffers (c point
+    // sets, two state scratch buffers, the staged checkpoint, the two adjoint
+    // buffers) are set aside.
+    const size_t mbytes = 3 * h->n * lbm::macro_bytes(h->prec);
+    int mt = 0;
+    if (h->cfg.adjoint_tail_segments >= 0) {
+        const size_t abytes = (size_t)lbm::Q * h->n * adj_bytes(h);
+        size_t reserve = ((size_t)1 << 30);
+        if (s.mseg.size() < (size_t)c) reserve += ((size_t)c - s.mseg.size()) * mbytes;
+        if (!s.mtmp[0]) reserve += 2 * fbytes;
+        if (!s.q0) reserve += fbytes;
+        if (!s.adj[0]) reserve += 2 * abytes + (size_t)h->dim * h->dim * sizeof(double);
+        const size_t r = device_room(h);
+        if (r > reserve) mt = (int)std::min<size_t>((size_t)nck, (r - reserve) / ((size_t)c * mbytes));
+        if (h->cfg.adjoint_tail_segments > 0) mt = std::min(mt, h->cfg.adjoint_tail_segments);
+    }
+    s.tail_k0 = (nck - mt) * c;
+    if (s.tail_k0 < iterations) {
+        const size_t bytes = (size_t)(iterations - s.tail_k0) * mbytes;
+        if (alloc_tracked(h, &s.tail_block, bytes) != LBM_OK) {
+            // not after all: recompute every segment
+            cudaGetLastError();
+            s.tail_block = nullptr;
+            s.tail_k0 = iterations;
+        } else {
+            s.tail_bytes = bytes;
+            for (int k = s.tail_k0; k < iterations; ++k)
+                s.tpts.push_back(static_cast<char *>(s.tail_block) + (size_t)(k - s.tail_k0) * mbytes);
+        }
+    }
+
     // Q_0, then the iterations, copying Q_{jc} into checkpoint j; runs that
-    // stay inside one checkpoint interval replay the step graph
+    // stay inside one checkpoint interval replay the step graph; the tail's
+    // iterations also store their points
     ADJ_CUDA(cudaMemcpyAsync(s.ckpt[0], h->f[h->cur], fbytes, cudaMemcpyDeviceToDevice, h->stream));
     for (int k = 0; k < iterations;) {
         const int G = h->graph_iters, next_ck = (k / c + 1) * c;
-        if (G > 1 && k + G <= iterations && k + G <= next_ck) {
+        if (k >= s.tail_k0) {
+            ADJ_CUDA(lbm::launch_iteration_adj(h, h->f[h->cur], h->f[h->cur ^ 1], s.tpts[k - s.tail_k0]));
+            h->cur ^= 1;
+            ++k;
+        } else if (G > 1 && k + G <= iterations && k + G <= next_ck) {
             ADJ_CUDA(lbm::replay_iterations(h));
             k += G;
         } else {
@@ -707,26 +777,16 @@ int lbm_adjoint_backward(lbm_t *h, double dloss, double *grad_tau, double *grad_
     const int T = s.iterations, c = s.every;
     const size_t fbytes = (size_t)lbm::Q * h->n * lbm::storage_bytes(h->prec);
     const size_t mbytes = 3 * h->n * lbm::macro_bytes(h->prec);
-    size_t freeb = 0, totalb = 0;
-    // device bytes this sweep may still take: free memory less a margin for
-    // the runtime and other users, within the handle's budget
-    auto room = [&]() -> size_t {
-        if (cudaMemGetInfo(&freeb, &totalb) != cudaSuccess) return 0;
-        const size_t margin = ((size_t)1 << 30) + totalb / 50;
-        size_t r = freeb > margin ? freeb - margin : 0;
-        const size_t cap = h->cfg.max_device_bytes;
-        if (cap > 0) {
-            const size_t used = h->base_bytes + s.bytes;
-            r = std::min(r, cap > used ? cap - used : (size_t)0);
-        }
-        return r;
-    };
+    // device bytes this sweep may still take
+    auto room = [&]() -> size_t { return device_room(h); };
 
     // Without a tau gradient the adjoint needs only the velocity of the FLUID
     // sites and the density of the lid sites of each iteration: the segments
     // are recomputed storing those three planes (c of them, plus two state
     // scratch buffers) instead of c - 1 full states.
     bool macro = grad_tau == nullptr && !h->cfg.adjoint_full_states;
+    // the recorded tail points serve the stored-point sweep only
+    if (!macro) free_tail_points(h);
     if (macro) {
         // the full-state buffers of an earlier sweep make room first (and
         // the graphs that captured them go)
@@ -737,6 +797,7 @@ int lbm_adjoint_backward(lbm_t *h, double dloss, double *grad_tau, double *grad_
                             (s.mtmp[0] ? 0 : 2 * fbytes);
         if (need > room()) {
             macro = false;  // does not fit: the full-state sweep (recursive when short)
+            free_tail_points(h);
         } else {
             for (int k = 0; k < 2; ++k)
                 if (!s.mtmp[k]) {
@@ -801,6 +862,13 @@ int lbm_adjoint_backward(lbm_t *h, double dloss, double *grad_tau, double *grad_
     }
     for (int j = nck - 1; j >= 0; --j) {
         const int start = j * c, len = std::min(T, start + c) - start;
+        if (macro && start >= s.tail_k0) {
+            // points recorded by the forward: the adjoint steps only
+            const int rc = adjoint_steps_down(h, start, len,
+                                              [&](int k) -> const void * { return s.tpts[k - s.tail_k0]; }, cur, true);
+            if (rc != LBM_OK) return rc;
+            continue;
+        }
         if (graphs && len == c) {
             ADJ_CUDA(cudaMemcpyAsync(s.q0, s.ckpt[j], fbytes, cudaMemcpyDeviceToDevice, st));
             const int rc = replay_segment(h, c, cur, macro);

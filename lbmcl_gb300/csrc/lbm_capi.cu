@@ -288,21 +288,24 @@ bool macro_within(int64_t it0, int G, int macro_every)
     return next <= it0 + G;
 }
 
-// One plain iteration of the direct / narrow variants inside a graph capture:
-// the face-row launch on the side stream, forked from and joined back into
-// the capture stream, so the graph runs it beside the interior-row launch
-// (they write disjoint rows of the output and read the same input).
-cudaError_t capture_split_iteration(const lbm_t *h, const lbm::StepArgs &a)
+bool splits(const lbm_t *h) { return h->kernel == LBM_KERNEL_DIRECT || h->kernel == LBM_KERNEL_NARROW; }
+
+// One iteration (MODE_STEP or MODE_STEP_ADJ) of the direct / narrow variants
+// with its face-row launch on the side stream, forked from and joined back
+// into the handle's stream, so that (in a captured graph: as a second
+// branch) it runs beside the interior-row launch; the two write disjoint rows
+// of the output and read the same input.
+cudaError_t split_iteration(const lbm_t *h, int mode, const lbm::StepArgs &a)
 {
     cudaError_t e = cudaEventRecord(h->ev_fork, h->stream);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(h->side, h->ev_fork, 0);
     if (e != cudaSuccess) return e;
     const int vb = h->kernel == LBM_KERNEL_NARROW ? 8 : 16;
     switch (h->prec) {
-    case LBM_FP32: e = lbm::launch_split_f32(vb, a, h->block, h->stream, h->side); break;
-    case LBM_FP64: e = lbm::launch_split_f64(vb, a, h->block, h->stream, h->side); break;
-    case LBM_FP16: e = lbm::launch_split_f16(vb, a, h->block, h->stream, h->side); break;
-    default: e = lbm::launch_split_bf16(vb, a, h->block, h->stream, h->side); break;
+    case LBM_FP32: e = lbm::launch_split_f32(vb, mode, a, h->block, h->stream, h->side); break;
+    case LBM_FP64: e = lbm::launch_split_f64(vb, mode, a, h->block, h->stream, h->side); break;
+    case LBM_FP16: e = lbm::launch_split_f16(vb, mode, a, h->block, h->stream, h->side); break;
+    default: e = lbm::launch_split_bf16(vb, mode, a, h->block, h->stream, h->side); break;
     }
     // join even after a failed launch, so the capture can end
     const cudaError_t ej = cudaEventRecord(h->ev_join, h->side);
@@ -319,18 +322,13 @@ cudaError_t replay_graph(lbm_t *h)
 {
     cudaGraphExec_t &exec = h->graph_exec[parity(h)];
     if (!exec) {
-        const bool split = h->kernel == LBM_KERNEL_DIRECT || h->kernel == LBM_KERNEL_NARROW;
-        if (split && !h->side) {
-            cudaError_t e = cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking);
-            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming);
-            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming);
-            if (e != cudaSuccess) return e;
-        }
+        const bool split = splits(h);
         cudaError_t e = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal);
         if (e != cudaSuccess) return e;
         int cur = h->cur, ph = h->aa_phase;
         for (int k = 0; k < h->graph_iters && e == cudaSuccess; ++k) {
-            e = split ? capture_split_iteration(h, step_args(h, cur, ph)) : launch_pull(h, lbm::MODE_STEP, step_args(h, cur, ph));
+            e = split ? split_iteration(h, lbm::MODE_STEP, step_args(h, cur, ph))
+                      : launch_pull(h, lbm::MODE_STEP, step_args(h, cur, ph));
             if (is_aa(h)) ph ^= 1;
             else cur ^= 1;
         }
@@ -357,7 +355,7 @@ cudaError_t launch_iteration(const lbm_t *h, const void *fin, void *fout)
     StepArgs a = step_args(h, h->cur);
     a.fin = fin;
     a.fout = fout;
-    return launch_pull(h, MODE_STEP, a);
+    return splits(h) ? split_iteration(h, MODE_STEP, a) : launch_pull(h, MODE_STEP, a);
 }
 
 cudaError_t launch_iteration_adj(const lbm_t *h, const void *fin, void *fout, void *point)
@@ -367,7 +365,7 @@ cudaError_t launch_iteration_adj(const lbm_t *h, const void *fin, void *fout, vo
     a.fout = fout;
     a.rho = nullptr;
     a.u = point;
-    return launch_pull(h, MODE_STEP_ADJ, a);
+    return splits(h) ? split_iteration(h, MODE_STEP_ADJ, a) : launch_pull(h, MODE_STEP_ADJ, a);
 }
 }  // namespace lbm
 
@@ -444,6 +442,8 @@ int lbm_init(lbm_t **out, const lbm_config *c)
         c->adjoint_kernel != LBM_KERNEL_STAGED)
         return fail(LBM_EINVAL, "lbm_init: adjoint_kernel %d must be 0, LBM_KERNEL_DIRECT or LBM_KERNEL_STAGED",
                     c->adjoint_kernel);
+    if (c->adjoint_tail_segments < -1)
+        return fail(LBM_EINVAL, "lbm_init: adjoint_tail_segments %d must be >= -1", c->adjoint_tail_segments);
     if (c->order < LBM_ORDER_REFERENCE || c->order > LBM_ORDER_SAILFISH)
         return fail(LBM_EINVAL, "lbm_init: unknown summation order %d", c->order);
     if (c->order == LBM_ORDER_SAILFISH && c->precision != LBM_FP32 && c->precision != LBM_FP64)
@@ -515,6 +515,9 @@ int lbm_init(lbm_t **out, const lbm_config *c)
         h->num_sms = prop.multiProcessorCount;
         h->graph_iters = c->graph_iterations == 0 ? 16 : c->graph_iterations;
         LBM_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+        LBM_CUDA(cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking));
+        LBM_CUDA(cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming));
+        LBM_CUDA(cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming));
         LBM_CUDA(cudaEventCreate(&h->ev_first));
         LBM_CUDA(cudaEventCreate(&h->ev_last));
         LBM_CUDA(cudaMalloc(&h->f[0], fbytes));

@@ -39,6 +39,13 @@ struct lbm_adjoint_state {
     // iteration of one segment (3 planes each) and two state scratch buffers
     std::vector<void *> mseg;
     void *mtmp[2] = {nullptr, nullptr};
+    // the points of the iterations tail_k0 .. T-1 (the last segments),
+    // recorded by the adjoint forward into one allocation: those segments
+    // are not recomputed
+    void *tail_block = nullptr;
+    size_t tail_bytes = 0;
+    std::vector<void *> tpts;  // per iteration, into tail_block
+    int tail_k0 = 0;
 };
 
 struct lbm_handle {

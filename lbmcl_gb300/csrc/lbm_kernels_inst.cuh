@@ -113,14 +113,16 @@ cudaError_t LBM_CAT(launch_pull_, LBM_SFX)(int mode, const StepArgs &a, unsigned
     return launch_direct<16>(mode, a, block, s, nparts);
 }
 
-// One plain iteration of the direct variant (VB = 16) or the narrow one
-// (VB = 8) with the face-row launch on stream sf, so that a graph captured
-// across the two streams runs the two launches side by side.
-cudaError_t LBM_CAT(launch_split_, LBM_SFX)(int vb, const StepArgs &a, unsigned block, cudaStream_t s, cudaStream_t sf)
+// One iteration (MODE_STEP or MODE_STEP_ADJ) of the direct variant (VB =
+// 16) or the narrow one (VB = 8) with the face-row launch on stream sf, so
+// that the two launches can run side by side.
+cudaError_t LBM_CAT(launch_split_, LBM_SFX)(int vb, int mode, const StepArgs &a, unsigned block, cudaStream_t s,
+                                            cudaStream_t sf)
 {
-    if (vb == 16) return launch_direct<16>(MODE_STEP, a, block, s, nullptr, 3, sf);
+    if (mode != MODE_STEP && mode != MODE_STEP_ADJ) return cudaErrorInvalidValue;
+    if (vb == 16) return launch_direct<16>(mode, a, block, s, nullptr, 3, sf);
     if constexpr (sizeof(LBM_S) < 8) {
-        if (vb == 8) return launch_direct<8>(MODE_STEP, a, block, s, nullptr, 3, sf);
+        if (vb == 8) return launch_direct<8>(mode, a, block, s, nullptr, 3, sf);
     }
     return cudaErrorInvalidValue;
 }

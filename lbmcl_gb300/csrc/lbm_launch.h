@@ -16,7 +16,7 @@ struct DumpArgs;
     cudaError_t launch_pull_##SFX(int mode, const StepArgs &a, unsigned block, cudaStream_t s,       \
                                   unsigned *nparts);                                                 \
     cudaError_t launch_narrow_##SFX(int mode, const StepArgs &a, unsigned block, cudaStream_t s);    \
-    cudaError_t launch_split_##SFX(int vb, const StepArgs &a, unsigned block, cudaStream_t s,         \
+    cudaError_t launch_split_##SFX(int vb, int mode, const StepArgs &a, unsigned block, cudaStream_t s,\
                                    cudaStream_t sf);                                                 \
     cudaError_t launch_aa_##SFX(int mode, const StepArgs &a, unsigned block, cudaStream_t s,         \
                                 unsigned *nparts);                                                   \

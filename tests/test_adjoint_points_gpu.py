@@ -15,6 +15,8 @@ def case(dim, seed):
 
 
 def grads(capi, prec, dim, iters, every, want_tau, **kw):
+    # the recompute paths unless a test asks for recorded tail points
+    kw.setdefault("adjoint_tail_segments", -1)
     lid, target = case(dim, dim + iters)
     with capi.Lattice(dim, velocity=0.0, precision=prec, lid=lid, tau=0.53, seed=3, noise_sigma=1e-4, **kw) as L:
         L.adjoint_set_loss(dim // 2, target)
@@ -47,7 +49,7 @@ def test_point_sweep_graph_replay_is_exact(capi, prec, steps):
     res = []
     for g in (0, 1):
         with capi.Lattice(dim, velocity=0.0, precision=prec, lid=lid, tau=0.53, seed=6, noise_sigma=1e-4,
-                          adjoint_steps=steps, graph_iterations=g) as L:
+                          adjoint_steps=steps, graph_iterations=g, adjoint_tail_segments=-1) as L:
             L.adjoint_set_loss(12, target)
             f0 = L.f()
             out = []
@@ -194,3 +196,23 @@ def test_staged_two_step_adjoint(capi, prec, dim, iters, every):
         assert np.abs(staged[2] - ref[2]).max() <= 1e-6 * np.abs(ref[2]).max()
         assert np.abs(staged[3] - ref[3]).max() <= 1e-6 * np.abs(ref[3]).max()
     assert np.abs(staged[2]).max() > 0 and np.isfinite(staged[3]).all()
+
+
+@pytest.mark.parametrize("prec,steps", [("fp32", 2), ("fp16", 2), ("bf16", 1), ("fp64", 1)])
+@pytest.mark.parametrize("dim,iters,every", [(24, 37, 8), (40, 20, 10)])
+def test_recorded_tail_points_are_exact(capi, prec, steps, dim, iters, every):
+    """Segments whose linearisation points the adjoint forward recorded (all
+    of them, two, or one) skip the recompute in the backward sweep: the
+    same loss and gradients bit for bit as recomputing every segment; with a
+    tau gradient (full-state sweep) the recorded points are not used."""
+    ref = grads(capi, prec, dim, iters, every, False, adjoint_steps=steps, adjoint_tail_segments=-1)
+    for tail in (0, 2, 1):
+        got = grads(capi, prec, dim, iters, every, False, adjoint_steps=steps, adjoint_tail_segments=tail)
+        assert got[0] == ref[0] and got[1] is None
+        np.testing.assert_array_equal(got[2], ref[2])
+        np.testing.assert_array_equal(got[3], ref[3])
+    full = grads(capi, prec, dim, iters, every, True, adjoint_steps=steps, adjoint_tail_segments=-1)
+    tail = grads(capi, prec, dim, iters, every, True, adjoint_steps=steps, adjoint_tail_segments=0)
+    assert full[1] == tail[1]
+    np.testing.assert_array_equal(full[2], tail[2])
+    np.testing.assert_array_equal(full[3], tail[3])

@@ -58,6 +58,7 @@ def _init(libonly, **kw):
     (dict(order=1, precision=3), "Sailfish"),   # FP16 storage: its own deviation sums
     (dict(adjoint_kernel=3), "adjoint_kernel"),  # only auto, direct or staged
     (dict(adjoint_kernel=-1), "adjoint_kernel"),
+    (dict(adjoint_tail_segments=-2), "adjoint_tail_segments"),
 ])
 def test_init_rejects_bad_arguments(libonly, kw, frag):
     rc, msg = _init(libonly, **kw)
