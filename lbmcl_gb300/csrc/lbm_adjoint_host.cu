@@ -661,8 +661,9 @@ int lbm_adjoint_forward(lbm_t *h, int iterations, int checkpoint_every, double *
     if (s.tail_k0 < iterations) {
         const size_t bytes = (size_t)(iterations - s.tail_k0) * mbytes;
         if (alloc_tracked(h, &s.tail_block, bytes) != LBM_OK) {
-            // not after all: recompute every segment
+            // not after all: recompute every segment (not an error of this call)
             cudaGetLastError();
+            lbm::set_last_error("");
             s.tail_block = nullptr;
             s.tail_k0 = iterations;
         } else {
