@@ -31,11 +31,14 @@ def main(argv=None) -> int:
     ap.add_argument("--tau", action="store_true", help="the adjoint also forms dJ/dtau (full-state segments)")
     ap.add_argument("--adjoint-kernel", default="auto", choices=["auto", "direct", "staged"],
                     help="two-step adjoint of the stored-point sweep: per-thread loads or TMA-staged planes")
+    ap.add_argument("--adjoint-tail", type=int, default=0,
+                    help="trailing segments whose points the adjoint forward records (0 = as many as fit, -1 = none)")
     a = ap.parse_args(argv)
     with capi.Lattice(a.dim, a.viscosity, a.velocity, precision=a.precision, stride=0, seed=a.seed,
                       noise_sigma=a.noise, block_threads=a.block, profile_steps=True, kernel=a.kernel,
                       stages=a.stages, adjoint_steps=a.adjoint_steps,
-                      adjoint_max_states=a.adjoint_max_states, adjoint_kernel=a.adjoint_kernel) as L:
+                      adjoint_max_states=a.adjoint_max_states, adjoint_kernel=a.adjoint_kernel,
+                      adjoint_tail_segments=a.adjoint_tail) as L:
         t0 = time.perf_counter()
         L.step(a.steps, every=a.every)
         L.sync()
