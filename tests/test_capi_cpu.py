@@ -125,3 +125,28 @@ def test_noalloc_checks_arguments_before_cuda(libonly, which):
     rc = fn(C.c_void_p(ptrs["f"]), C.c_void_p(ptrs["map"]), C.c_void_p(ptrs["lid"]), dim, libonly.FP32, None, out)
     assert rc == libonly.EINVAL
     assert ("dim 4096" if which == "dim" else "misaligned") in L.lbm_last_error().decode()
+
+
+def test_config_layout_matches_the_binding(tmp_path):
+    """The ctypes Config of the Python binding has the C struct's size and
+    every field at the C offset (fields are only ever appended)."""
+    import shutil
+    from lbmcl_gb300 import capi
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+    names = [f for f, _ in capi.Config._fields_]
+    body = "".join(f'    printf("%s %zu\\n", "{f}", offsetof(lbm_config, {f}));\n' for f in names)
+    src = tmp_path / "layout.c"
+    src.write_text('#include <stddef.h>\n#include <stdio.h>\n#include "lbm.h"\nint main(void) {\n'
+                   '    printf("sizeof %zu\\n", sizeof(lbm_config));\n' + body + "    return 0;\n}\n")
+    exe = tmp_path / "layout"
+    r = subprocess.run([cc, "-std=c99", "-I" + inc, str(src), "-o", str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = dict(line.split() for line in subprocess.run([str(exe)], capture_output=True, text=True,
+                                                        check=True).stdout.splitlines())
+    import ctypes as C
+    assert int(out["sizeof"]) == C.sizeof(capi.Config)
+    for f in names:
+        assert int(out[f]) == getattr(capi.Config, f).offset, f
