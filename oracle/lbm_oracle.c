@@ -100,7 +100,8 @@ void lbmo_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t o
 /* ln(x) for finite x > 0 in single precision: x = m 2^e with m in
  * [sqrt(1/2), sqrt(2)), ln m = 2 atanh(s), s = (m-1)/(m+1), summed as the odd
  * series 2 s (1 + s^2/3 + ... + s^12/13) (|s| <= 0.1716: truncation below
- * 1e-9).  IEEE float + - * / only, no library call. */
+ * 1e-9) by Horner steps with fused multiply-adds.  IEEE float + - * / and
+ * fmaf (one rounding, as the GPU's fma) only. */
 float lbmo_logf(float x)
 {
     uint32_t bits;
@@ -121,30 +122,31 @@ float lbmo_logf(float x)
     static const float inv_odd[7] = {1.0f / 1.0f, 1.0f / 3.0f, 1.0f / 5.0f, 1.0f / 7.0f,
                                      1.0f / 9.0f, 1.0f / 11.0f, 1.0f / 13.0f};
     float acc = inv_odd[6];
-    for (int k = 5; k >= 0; --k) acc = inv_odd[k] + s2 * acc;
+    for (int k = 5; k >= 0; --k) acc = fmaf(s2, acc, inv_odd[k]);
     const float ln2 = 0.693147182f;
-    return ((float)e * ln2) + ((2.0f * s) * acc);
+    return fmaf(2.0f * s, acc, (float)e * ln2);
 }
 
 double lbmo_log(double x) { return (double)lbmo_logf((float)x); }
 
 /* cos and sin of 2 pi (k/4 + 1/8) + x, x in (-pi/4, pi/4), k in 0..3:
- * Taylor series of cos x (to x^10) and sin x (to x^9), the rotation by pi/4
- * to pi/4 + x, then the quarter turn k.  IEEE float + - * only. */
+ * Taylor series of cos x (to x^10) and sin x (to x^9) by Horner steps with
+ * fused multiply-adds, the rotation by pi/4 to pi/4 + x, then the quarter
+ * turn k.  IEEE float + - * and fmaf only. */
 static void lbmo_quarter_turn_cs(uint32_t k, float x, float *c, float *s)
 {
     const float x2 = x * x;
     float sp = 1.0f / 362880.0f;
-    sp = (-1.0f / 5040.0f) + x2 * sp;
-    sp = (1.0f / 120.0f) + x2 * sp;
-    sp = (-1.0f / 6.0f) + x2 * sp;
-    const float sn = x + (x * x2) * sp;
+    sp = fmaf(x2, sp, -1.0f / 5040.0f);
+    sp = fmaf(x2, sp, 1.0f / 120.0f);
+    sp = fmaf(x2, sp, -1.0f / 6.0f);
+    const float sn = fmaf(x * x2, sp, x);
     float cp = -1.0f / 3628800.0f;
-    cp = (1.0f / 40320.0f) + x2 * cp;
-    cp = (-1.0f / 720.0f) + x2 * cp;
-    cp = (1.0f / 24.0f) + x2 * cp;
-    cp = -0.5f + x2 * cp;
-    const float cs = 1.0f + x2 * cp;
+    cp = fmaf(x2, cp, 1.0f / 40320.0f);
+    cp = fmaf(x2, cp, -1.0f / 720.0f);
+    cp = fmaf(x2, cp, 1.0f / 24.0f);
+    cp = fmaf(x2, cp, -0.5f);
+    const float cs = fmaf(x2, cp, 1.0f);
     const float h = 0.707106781f; /* sqrt(1/2) */
     const float c0 = h * (cs - sn), s0 = h * (cs + sn);
     *c = (k == 0) ? c0 : (k == 1) ? -s0 : (k == 2) ? -c0 : s0;
@@ -170,7 +172,7 @@ static void lbmo_box_muller(uint32_t w0, uint32_t w1, float z[2])
 /* Two standard normals for (seed, site, pair) by the Box-Muller transform:
  * Philox4x32-10 on the counter (site_lo, site_hi, pair >> 1, 0); words 0, 1
  * give pair 2g, words 2, 3 pair 2g + 1 of block g.  Single precision, IEEE
- * + - * / sqrt only. */
+ * + - * / sqrt and fmaf only. */
 void lbmo_gauss_pairf(uint64_t seed, uint64_t site, uint32_t pair, float z[2])
 {
     const uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
