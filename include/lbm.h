@@ -200,7 +200,10 @@ int lbm_iteration(const lbm_t *h, int64_t *it);
 const char *lbm_device_name(const lbm_t *h);
 
 /* The handle's CUDA stream (cudaStream_t), for callers that time or order
- * their own work against it. */
+ * their own work against it.  (Iterations may run their face-row launches
+ * on a second internal stream; that work is always joined back into this
+ * stream, so ordering against it orders against everything the handle
+ * enqueued.) */
 void *lbm_stream(lbm_t *h);
 
 /* FP64 sums over the sites that store macros (FLUID and MOVING) of the
